@@ -1,0 +1,421 @@
+#!/usr/bin/env python3
+"""Barnes-Hut step throughput of the GB300 library.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step" = bbox -> build -> summarize -> sort -> force+Euler on
+the whole system): N = 4,194,304 bodies, positions normal with
+sigma = (1, 1, 0.2), lognormal(0, 0.5) masses normalised to 1, zero
+velocities, G = 1, theta = 0.5, eps = 0.005, dt = 1e-3, compensated force
+accumulation, seeded synthetic data.  Metric: body-updates/s.
+
+`value` is device time (CUDA events on the library's stream) with the bodies
+resident in HBM; `e2e` goes through the public C ABI every step:
+nb_set_state from pinned host arrays, nb_step, nb_get_state into pinned host
+arrays.  The accuracy gate (RMS relative force error vs an FP64 direct sum
+on 8192 sample bodies <= 1e-3) is evaluated after the timed region.
+
+Under torchrun (--gpus N > 1) every rank advances its own independent
+system on its own GPU (replicas; no exchange); rank 0 prints the aggregate.
+--impl reference times the CPU restatement of the reference's kernels
+(oracle/, OpenMP) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="bh_plummer_n4m_theta0.5", n=4194304, sigma=(1.0, 1.0, 0.2), mass_sigma=0.5, theta=0.5,
+                eps=0.005, dt=1e-3, G=1.0, precision="compensated")
+PROBE_SAMPLES = 8192
+FP32_LANES_PER_SM = 128
+FLOPS_PER_INTERACTION = 12  # FP32-pipe instructions per interaction (3 sub, 3 fma, 3 mul, 3 fma)
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (host-side only: barriers and a max over ranks)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def device_sm_count(dev: int) -> int:
+    """Multiprocessor count from the CUDA driver API."""
+    drv = ctypes.CDLL("libcuda.so.1")
+    drv.cuInit(0)
+    h = ctypes.c_int(0)
+    drv.cuDeviceGet(ctypes.byref(h), dev)
+    v = ctypes.c_int(0)
+    drv.cuDeviceGetAttribute(ctypes.byref(v), 16, h)  # CU_DEVICE_ATTRIBUTE_MULTIPROCESSOR_COUNT
+    return v.value
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def workload_ic(nb, n, seed):
+    cfg = nb.default_config(num_of_bodies=n, pos_config=nb.NORMAL_SIGMA_POS, pos_sigma=WORKLOAD["sigma"],
+                            mass_config=nb.MASS_LOGNORMAL, mass_lognormal_sigma=WORKLOAD["mass_sigma"],
+                            vel_config=nb.FUNC_ZERO_VEL, seed=seed)
+    pos, _, mass = nb.generate_ic(cfg)
+    vel = np.zeros_like(pos)
+    return pos, vel, mass
+
+
+def make_sim(nb, n, precision, device):
+    return nb.Simulation(num_of_bodies=n, algo_config=nb.BARNES_HUT, theta=WORKLOAD["theta"],
+                         epsilon=WORKLOAD["eps"], gravitational_constant=WORKLOAD["G"], numerical_method=nb.EULER,
+                         precision=precision, device=device)
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's restatement of the reference kernels, sampled
+# ---------------------------------------------------------------------------
+def cpu_baseline(pos, mass, sample_groups=512, repeats=1):
+    """bbox + build + summarise + sort over all N bodies (sequential C, as the
+    oracle restates them) plus the force walk (OpenMP) for `sample_groups`
+    warp groups of 32 spread over the sorted order, scaled to N."""
+    from oracle import oracle as O
+    O.build()
+    n = len(mass)
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        box = O.bbox_exact(pos)
+        t = O.tree_build(O.SEM_GEOMETRIC, pos, mass, box, 2 * n)
+        O.saturate(t)
+        srt, _ = O.sort_bodies(t.children, n, t.root)
+        t1 = time.perf_counter()
+        dq = O.thresholds(O.CRIT_STANDARD, box, WORKLOAD["theta"], WORKLOAD["eps"], t.max_depth)
+        ngroups = n // 32
+        pick = np.linspace(0, ngroups - 1, sample_groups).astype(np.int64)
+        order = (pick[:, None] * 32 + np.arange(32)[None, :]).ravel()
+        order = srt[order]
+        t2 = time.perf_counter()
+        O.bh_force(t, dq, WORKLOAD["eps"], WORKLOAD["G"], vote_width=32, order=order, compensated=True)
+        t3 = time.perf_counter()
+        step = (t1 - t0) + (t3 - t2) * (n / len(order))
+        times.append(step)
+    step = min(times)
+    return {"value": n / step, "unit": "body-updates/s", "cores": int(O.lib().orc_max_threads()), "kind": "port",
+            "sample": (f"N={n}: bbox+build+summarize+sort on all bodies (sequential C), force walk "
+                       f"(OpenMP, {O.lib().orc_max_threads()} threads) on {sample_groups} warp groups "
+                       f"({len(order)} bodies) scaled to N; {step:.2f} s per step"),
+            "seconds_per_step": step}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, dist: Dist):
+    from nbodysimulation_gb300 import build as nbbuild
+    if dist.local_rank == 0:
+        nbbuild.build()
+    dist.barrier()
+    import nbodysimulation_gb300 as nb
+    L = nb.load()
+    n, dt = WORKLOAD["n"], WORKLOAD["dt"]
+    dev = dist.local_rank
+    pos, vel, mass = workload_ic(nb, n, seed=dist.rank)
+    sim = make_sim(nb, n, nb.PRECISION_COMPENSATED, dev)
+    sim.set_state(pos, mass, vel)
+    sim.set_profiling(True)
+    sim.step(dt, args.warmup)
+
+    # --- value: bodies resident in HBM, CUDA events on the library stream ---
+    clocks = ClockSampler(dev)
+    launches0 = sim.kernel_launches()
+    dist.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    ms = sim.time_steps(dt, args.steps)
+    clk = clocks.stop()
+    dist.barrier()
+    launches = sim.kernel_launches() - launches0
+    stage = sim.timings()
+    inter, opened = sim.work_counters()
+    info = sim.stage_debug(nb.DEBUG_TREE_INFO)
+    cells_used = int(info[0] + info[1] - info[2] + 1)
+    ms_max = dist.max(ms)
+    total_bodies = dist.sum(float(n))
+    value = total_bodies * args.steps / (ms_max / 1e3)
+
+    # --- e2e through the C ABI with pinned host buffers ---
+    hp = [L.nb_host_alloc(12 * n), L.nb_host_alloc(12 * n), L.nb_host_alloc(4 * n), L.nb_host_alloc(12 * n),
+          L.nb_host_alloc(12 * n)]
+    if not all(hp):
+        raise RuntimeError("nb_host_alloc failed")
+    ctypes.memmove(hp[0], pos.ctypes.data, 12 * n)
+    ctypes.memmove(hp[1], vel.ctypes.data, 12 * n)
+    ctypes.memmove(hp[2], mass.ctypes.data, 4 * n)
+    sim.set_profiling(False)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = L.nb_set_state(sim.h, hp[0], hp[1], hp[2], n)
+        st = st or L.nb_step(sim.h, dt, 1)
+        st = st or L.nb_get_state(sim.h, hp[3], hp[4], None, None)
+        if st:
+            raise RuntimeError(f"e2e step failed: {L.nb_last_error_message(sim.h).decode()}")
+    e2e_s = time.perf_counter() - t0
+    dist.barrier()
+    e2e_s = dist.max(e2e_s)
+    for p in hp:
+        L.nb_host_free(p)
+    e2e_value = total_bodies * args.steps / e2e_s
+
+    # --- accuracy gate (after the timed regions) ---
+    rng = np.random.default_rng(1234)
+    sample = rng.choice(n, PROBE_SAMPLES, replace=False).astype(np.int32)
+    err_max, err_rms, _ = sim.force_error(sample)
+
+    # --- plain FP32 accumulation, same workload, for reference ---
+    fp32_value = None
+    if not args.skip_fp32:
+        sim.close()
+        sim2 = make_sim(nb, n, nb.PRECISION_FP32, dev)
+        sim2.set_state(pos, mass, vel)
+        sim2.step(dt, args.warmup)
+        ms2 = sim2.time_steps(dt, args.steps)
+        fp32_value = total_bodies * args.steps / (dist.max(ms2) / 1e3)
+        sim2.close()
+    else:
+        sim.close()
+
+    if dist.rank != 0:
+        return None
+    peaks, peak_kind = measured_peaks()
+    force_ms = stage["force"]
+    # algorithmic bytes of one force launch: per body sorted index 4 B, body
+    # {x,y,z,m} 16 B, velocity 16 B read; body, velocity, acceleration 48 B
+    # written; per cell in the tree its child list 32 B and packed child line
+    # 128 B read once
+    alg_bytes = 84 * n + 160 * cells_used
+    achieved = alg_bytes / (force_ms / 1e3) / 1e9
+    sm_mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    sm_count = device_sm_count(dev)
+    inter_per_step = inter / args.steps
+    fp32_peak = FP32_LANES_PER_SM * sm_count * sm_mhz * 1e6 / FLOPS_PER_INTERACTION
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "force_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            t = json.load(f)
+        traffic = t["bytes_per_body"] * n
+    out = {
+        "metric": "BH body-updates/s N=4M theta=0.5 (RMS force err <= 1e-3)",
+        "value": value,
+        "unit": "body-updates/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded normal sigma=(1,1,0.2) positions, lognormal masses)",
+        "config": {"workload": WORKLOAD["name"], "n_bodies": n, "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"],
+                   "dt": dt, "G": WORKLOAD["G"], "integrator": "euler", "precision": WORKLOAD["precision"],
+                   "tree": "geometric octree, standard opening criterion, 32-lane warp vote",
+                   "l2": "inputs larger than L2 (bodies + tree about 2.3 GB per system)",
+                   "parallelism": f"replicas x{dist.world}"},
+        "e2e": {"value": e2e_value, "unit": "body-updates/s", "h2d_bytes_per_step": 28 * n,
+                "d2h_bytes_per_step": 24 * n + 64},
+        "gpu_launches": int(launches),
+        "stages_ms": {k: round(v, 4) for k, v in stage.items() if v > 0},
+        "accuracy": {"rms_rel_err": err_rms, "max_rel_err": err_max, "samples": PROBE_SAMPLES,
+                     "oracle": "FP64 direct sum on the GPU", "gate_rms_le_1e-3": bool(err_rms <= 1e-3)},
+        "fp32_accumulation_value": fp32_value,
+        "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                     "algorithmic_bytes": alg_bytes, "peak_kind": f"{peak_kind} hbm copy",
+                     "note": "the force walk is latency / FP32-bound; see compute"},
+        "compute": {"bound": "fp32", "interactions_per_step": inter_per_step,
+                    "interactions_per_s": inter_per_step / (force_ms / 1e3),
+                    "peak_interactions_per_s": fp32_peak,
+                    "frac": (inter_per_step / (force_ms / 1e3)) / fp32_peak,
+                    "cells_opened_per_step": opened / args.steps,
+                    "peak_kind": "derived: 128 FP32 lanes x SMs x median sampled SM clock / 12"},
+        "tree": {"cells_used": cells_used, "max_depth": int(info[3])},
+        "clocks": clk,
+    }
+    if not args.skip_cpu:
+        out["cpu_baseline"] = cpu_baseline(pos, mass)
+    return out
+
+
+def run_reference(args, dist: Dist):
+    """The reference's CPU path as restated by the oracle, all host threads."""
+    if dist.rank != 0:
+        return None
+    import nbodysimulation_gb300 as nb
+    from nbodysimulation_gb300 import build as nbbuild
+    nbbuild.build()
+    n = WORKLOAD["n"]
+    pos, _, mass = workload_ic(nb, n, seed=0)
+    for _ in range(args.warmup):
+        cpu_baseline(pos, mass, sample_groups=64)
+    t0 = time.perf_counter()
+    per = []
+    for _ in range(args.steps):
+        per.append(cpu_baseline(pos, mass, sample_groups=128))
+    wall = time.perf_counter() - t0
+    step_s = sum(p["seconds_per_step"] for p in per) / len(per)
+    value = n / step_s
+    cb = dict(per[-1])
+    cb["value"] = value
+    return {
+        "impl": "reference",
+        "metric": "BH body-updates/s N=4M theta=0.5 (RMS force err <= 1e-3)",
+        "value": value,
+        "unit": "body-updates/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_s * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded normal sigma=(1,1,0.2) positions, lognormal masses)",
+        "config": {"workload": WORKLOAD["name"], "n_bodies": n, "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"],
+                   "dt": WORKLOAD["dt"], "precision": WORKLOAD["precision"], "wall_s": wall},
+        "cpu_baseline": cb,
+        "e2e": {"value": value, "unit": "body-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
+    ap.add_argument("--skip-fp32", action="store_true", help="omit the plain-FP32 accumulation run")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        out = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+        if dist.rank == 0 and out is not None:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,441 @@
+// k_direct.cu -- all-pairs kernels: the direct sums (update /
+// update_local, kernels/brute_force_update.cl), the collision update
+// (kernels/collision_update.cl) and copy_vertices (kernels/copy_vertices.cl),
+// plus the host-layout pack/unpack kernels.
+//
+// The tiled kernels stage j-tiles of packed {x,y,z,m} bodies into shared
+// memory with TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx),
+// double-buffered, no cluster and no multicast; each thread keeps kI target
+// bodies in registers so one broadcast shared-memory load feeds kI
+// interactions.  Small systems split the j range over gridDim.y blocks and
+// combine partial accelerations with float atomics before a separate
+// integrate pass.
+#include "nbgb_internal.cuh"
+
+namespace nbgb {
+
+constexpr int kTile = 256;        // bodies per staged tile (4 KiB)
+constexpr int kDirectThreads = 256;
+
+// ---- PTX helpers: mbarrier + bulk async copy (sm_90+) ----
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait on a tile; on timeout records the status and keeps waiting
+// (bounded again) so no copy into this block's shared memory is left in
+// flight when the block exits.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, Ctrl *ctrl) {
+    long long it = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if (++it > kSpinCap) {
+            set_status(ctrl, kStSpinTimeout, -1);
+            long long it2 = 0;
+            while (!mbar_try_wait(bar, parity) && ++it2 < kSpinCap) {
+            }
+            return false;
+        }
+    }
+    return true;
+}
+
+// ---- pair interactions ----
+template <bool kQuirk, bool kEpsZero>
+__device__ __forceinline__ void pair(const float4 me, const float4 q, float eps2, float &ax, float &ay, float &az) {
+    const float dx = q.x - me.x, dy = q.y - me.y, dz = q.z - me.z;
+    if constexpr (!kQuirk) {
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+        const float r = rsqrtf(d2);
+        float F = (q.w * r) * (r * r);
+        if constexpr (kEpsZero) F = d2 > 0.0f ? F : 0.0f;
+        ax = fmaf(dx, F, ax);
+        ay = fmaf(dy, F, ay);
+        az = fmaf(dz, F, az);
+    } else {
+        // the reference's brute-force arithmetic: n = normalize(r),
+        // s = m / (|n|^2 + e^2) (brute_force_update.cl:54-60, 114-123);
+        // the zero vector normalises to zero, so the self pair adds nothing
+        const float l2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float inv = l2 > 0.0f ? rsqrtf(l2) : 0.0f;
+        const float nx = dx * inv, ny = dy * inv, nz = dz * inv;
+        const float dist_sqr = fmaf(nz, nz, fmaf(ny, ny, fmaf(nx, nx, eps2)));
+        const float s = __fdividef(q.w, dist_sqr);
+        ax = fmaf(nx, s, ax);
+        ay = fmaf(ny, s, ay);
+        az = fmaf(nz, s, az);
+    }
+}
+
+template <int kMethod>
+__device__ __forceinline__ void integrate_one(const DevSim &s, const StepParams &p, int b, const float4 P, float ax,
+                                              float ay, float az) {
+    const float dt = p.dt;
+    const float4 v = s.vel[b];
+    float4 x = P, vo = v;
+    if constexpr (kMethod == 2) {
+        vo.x = __fadd_rn(v.x, __fmul_rn(ax, dt));
+        vo.y = __fadd_rn(v.y, __fmul_rn(ay, dt));
+        vo.z = __fadd_rn(v.z, __fmul_rn(az, dt));
+        x.x = __fadd_rn(P.x, __fmul_rn(vo.x, dt));
+        x.y = __fadd_rn(P.y, __fmul_rn(vo.y, dt));
+        x.z = __fadd_rn(P.z, __fmul_rn(vo.z, dt));
+        s.acc[b] = make_float4(ax, ay, az, 0.0f);
+    } else if constexpr (kMethod == 1) {
+        const float4 ap = s.acc[b];
+        const float hx = __fadd_rn(v.x, __fmul_rn(__fmul_rn(ap.x, dt), 0.5f));
+        const float hy = __fadd_rn(v.y, __fmul_rn(__fmul_rn(ap.y, dt), 0.5f));
+        const float hz = __fadd_rn(v.z, __fmul_rn(__fmul_rn(ap.z, dt), 0.5f));
+        x.x = __fadd_rn(P.x, __fmul_rn(hx, dt));
+        x.y = __fadd_rn(P.y, __fmul_rn(hy, dt));
+        x.z = __fadd_rn(P.z, __fmul_rn(hz, dt));
+        vo.x = __fadd_rn(hx, __fmul_rn(__fmul_rn(ax, dt), 0.5f));
+        vo.y = __fadd_rn(hy, __fmul_rn(__fmul_rn(ay, dt), 0.5f));
+        vo.z = __fadd_rn(hz, __fmul_rn(__fmul_rn(az, dt), 0.5f));
+    } else if constexpr (kMethod == 3) {
+        const float h = p.kdk_primed ? dt : __fmul_rn(dt, 0.5f);
+        vo.x = __fadd_rn(v.x, __fmul_rn(ax, h));
+        vo.y = __fadd_rn(v.y, __fmul_rn(ay, h));
+        vo.z = __fadd_rn(v.z, __fmul_rn(az, h));
+        x.x = __fadd_rn(P.x, __fmul_rn(vo.x, dt));
+        x.y = __fadd_rn(P.y, __fmul_rn(vo.y, dt));
+        x.z = __fadd_rn(P.z, __fmul_rn(vo.z, dt));
+        s.acc[b] = make_float4(ax, ay, az, 0.0f);
+    }
+    s.vel[b] = vo;
+    s.body_next[b] = x;
+}
+
+// ---------------------------------------------------------------------------
+// direct_global: one thread per body, j straight from global memory through
+// L1 (update, brute_force_update.cl:3-105).  The naive baseline.
+// ---------------------------------------------------------------------------
+template <int kMethod, bool kQuirk, bool kEpsZero>
+__global__ void __launch_bounds__(256) k_direct_global(DevSim s, StepParams p, float eps) {
+    const int n = s.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 me = s.body_cur[i];
+    const float eps2 = eps * eps;
+    float ax = 0.0f, ay = 0.0f, az = 0.0f;
+    for (int j = 0; j < n; ++j) {
+        const float4 q = __ldg(&s.body_cur[j]);
+        if (!kQuirk && kEpsZero && j == i) continue;
+        pair<kQuirk, false>(me, q, eps2, ax, ay, az);
+    }
+    integrate_one<kMethod>(s, p, i, me, ax * p.G, ay * p.G, az * p.G);
+}
+
+// ---------------------------------------------------------------------------
+// direct_tiled (update_local, brute_force_update.cl:128-228): TMA-staged
+// j-tiles.  The reference's tile loop reloads tile 0 and skips the wrong body
+// (:167-184); here every j is visited once.  gridDim.y > 1 splits the j range
+// and accumulates partial accelerations into `part` (float atomics).
+// ---------------------------------------------------------------------------
+template <int kI, int kMethod, bool kQuirk, bool kEpsZero>
+__global__ void __launch_bounds__(kDirectThreads) k_direct_tiled(DevSim s, StepParams p, float eps, float4 *part) {
+    __shared__ __align__(128) float4 tile[2][kTile];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int n = s.n;
+    const int ntiles = (n + kTile - 1) / kTile;
+    const int per_split = (ntiles + gridDim.y - 1) / gridDim.y;
+    const int t0 = blockIdx.y * per_split;
+    const int t1 = min(ntiles, t0 + per_split);
+    const float eps2 = eps * eps;
+    int idx[kI];
+    float4 me[kI];
+    float ax[kI], ay[kI], az[kI];
+#pragma unroll
+    for (int r = 0; r < kI; ++r) {
+        idx[r] = blockIdx.x * (kDirectThreads * kI) + r * kDirectThreads + threadIdx.x;
+        me[r] = idx[r] < n ? s.body_cur[idx[r]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        ax[r] = ay[r] = az[r] = 0.0f;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](int t, int stage) {
+        const int cnt = min(kTile, n - t * kTile);
+        const uint32_t bytes = (uint32_t)cnt * 16u;
+        mbar_expect_tx(&bar[stage], bytes);
+        bulk_g2s(&tile[stage][0], s.body_cur + (size_t)t * kTile, bytes, &bar[stage]);
+    };
+    if (threadIdx.x == 0 && t0 < t1) issue(t0, 0);
+    bool ok = true;
+    for (int t = t0; t < t1; ++t) {
+        const int it = t - t0;
+        const int stage = it & 1;
+        if (threadIdx.x == 0 && t + 1 < t1) issue(t + 1, stage ^ 1);
+        if (!mbar_wait_bounded(&bar[stage], (uint32_t)((it >> 1) & 1), s.ctrl)) ok = false;
+        const int cnt = min(kTile, n - t * kTile);
+        const float4 *tl = tile[stage];
+        if (cnt == kTile) {
+#pragma unroll 4
+            for (int j = 0; j < kTile; ++j) {
+                const float4 q = tl[j];
+#pragma unroll
+                for (int r = 0; r < kI; ++r) pair<kQuirk, kEpsZero>(me[r], q, eps2, ax[r], ay[r], az[r]);
+            }
+        } else {
+            for (int j = 0; j < cnt; ++j) {
+                const float4 q = tl[j];
+#pragma unroll
+                for (int r = 0; r < kI; ++r) pair<kQuirk, kEpsZero>(me[r], q, eps2, ax[r], ay[r], az[r]);
+            }
+        }
+        if (!__syncthreads_and(ok)) {
+            // drain the copy already issued for the next tile before leaving
+            if (threadIdx.x == 0 && t + 1 < t1)
+                mbar_wait_bounded(&bar[stage ^ 1], (uint32_t)(((it + 1) >> 1) & 1), s.ctrl);
+            ok = false;
+            break;
+        }
+    }
+    if (!ok) return;
+#pragma unroll
+    for (int r = 0; r < kI; ++r) {
+        if (idx[r] >= n) continue;
+        if (gridDim.y == 1) {
+            integrate_one<kMethod>(s, p, idx[r], me[r], ax[r] * p.G, ay[r] * p.G, az[r] * p.G);
+        } else {
+            atomicAdd(&part[idx[r]].x, ax[r]);
+            atomicAdd(&part[idx[r]].y, ay[r]);
+            atomicAdd(&part[idx[r]].z, az[r]);
+        }
+    }
+}
+
+template <int kMethod>
+__global__ void k_integrate_partial(DevSim s, StepParams p, const float4 *part) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    const float4 a = part[i];
+    integrate_one<kMethod>(s, p, i, s.body_cur[i], a.x * p.G, a.y * p.G, a.z * p.G);
+}
+
+// ---------------------------------------------------------------------------
+// collision (update_collision_local, collision_update.cl:17-83): for every
+// body, every other body in ascending index order; if |pi - pj| <= 0.015 +
+// 0.015, reflect v_i <- v_i - 2 (n.v_i) n, n = normalize(pj - pi)
+// (calc_collision_traj, :3-15).  The running v_i carries through the j
+// order, positions are read only.  Distance and reflection use separately
+// rounded operations and a correctly rounded 1/sqrt, so every decision and
+// every result matches the oracle bit for bit.  Reads the positions written
+// by the integrator of the same step (the reference runs it after the force
+// kernel, src/MyApp.cpp:593-596).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kDirectThreads) k_collision(DevSim s) {
+    __shared__ __align__(128) float4 tile[2][kTile];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int n = s.n;
+    const float4 *pos = s.body_next;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const float4 me = i < n ? pos[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 v = i < n ? s.vel[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float rr = 0.015f + 0.015f;
+    const int ntiles = (n + kTile - 1) / kTile;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](int t, int stage) {
+        const int cnt = min(kTile, n - t * kTile);
+        const uint32_t bytes = (uint32_t)cnt * 16u;
+        mbar_expect_tx(&bar[stage], bytes);
+        bulk_g2s(&tile[stage][0], pos + (size_t)t * kTile, bytes, &bar[stage]);
+    };
+    if (threadIdx.x == 0 && ntiles > 0) issue(0, 0);
+    bool ok = true;
+    for (int t = 0; t < ntiles; ++t) {
+        const int stage = t & 1;
+        if (threadIdx.x == 0 && t + 1 < ntiles) issue(t + 1, stage ^ 1);
+        if (!mbar_wait_bounded(&bar[stage], (uint32_t)((t >> 1) & 1), s.ctrl)) ok = false;
+        const int cnt = min(kTile, n - t * kTile);
+        for (int j = 0; j < cnt; ++j) {
+            const int jj = t * kTile + j;
+            const float4 q = tile[stage][j];
+            if (jj == i) continue;
+            const float ex = __fsub_rn(me.x, q.x), ey = __fsub_rn(me.y, q.y), ez = __fsub_rn(me.z, q.z);
+            const float dist = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez)));
+            if (dist > rr) continue;
+            float nx = __fsub_rn(q.x, me.x), ny = __fsub_rn(q.y, me.y), nz = __fsub_rn(q.z, me.z);
+            const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
+            if (l2 != 0.0f) {
+                const float inv = __fdiv_rn(1.0f, __fsqrt_rn(l2));
+                nx = __fmul_rn(nx, inv);
+                ny = __fmul_rn(ny, inv);
+                nz = __fmul_rn(nz, inv);
+            }
+            const float dp = __fadd_rn(__fadd_rn(__fmul_rn(nx, v.x), __fmul_rn(ny, v.y)), __fmul_rn(nz, v.z));
+            const float k2 = __fmul_rn(2.0f, dp);
+            v.x = __fsub_rn(v.x, __fmul_rn(k2, nx));
+            v.y = __fsub_rn(v.y, __fmul_rn(k2, ny));
+            v.z = __fsub_rn(v.z, __fmul_rn(k2, nz));
+        }
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0 && t + 1 < ntiles)
+                mbar_wait_bounded(&bar[stage ^ 1], (uint32_t)(((t + 1) >> 1) & 1), s.ctrl);
+            ok = false;
+            break;
+        }
+    }
+    if (ok && i < n) s.vel[i] = v;
+}
+
+__global__ void k_copy_vertices(const float4 *__restrict__ b, int n, float4 *__restrict__ dst) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = b[i];
+        dst[i] = make_float4(p.x, p.y, p.z, 1.0f);
+    }
+}
+
+__global__ void k_pack(const float *__restrict__ pos3, const float *__restrict__ mass, const float *__restrict__ vel3,
+                       float4 *body, float4 *vel, float4 *acc, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (pos3) {
+            const float m = mass ? mass[i] : body[i].w;
+            body[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], m);
+        } else if (mass) {
+            body[i].w = mass[i];
+        }
+        if (vel) vel[i] = vel3 ? make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0f)
+                               : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (acc) acc[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+__global__ void k_unpack(const float4 *__restrict__ body, const float4 *__restrict__ vel,
+                         const float4 *__restrict__ acc, float *pos3, float *vel3, float *acc3, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (pos3) {
+            const float4 p = body[i];
+            pos3[3 * i] = p.x; pos3[3 * i + 1] = p.y; pos3[3 * i + 2] = p.z;
+        }
+        if (vel3) {
+            const float4 v = vel[i];
+            vel3[3 * i] = v.x; vel3[3 * i + 1] = v.y; vel3[3 * i + 2] = v.z;
+        }
+        if (acc3) {
+            const float4 a = acc[i];
+            acc3[3 * i] = a.x; acc3[3 * i + 1] = a.y; acc3[3 * i + 2] = a.z;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <int kMethod, bool kQuirk, bool kEpsZero>
+static cudaError_t launch_direct_t(const DevSim &s, const StepParams &p, float eps, int tiled, int sm_count,
+                                   cudaStream_t st, float4 *part) {
+    const int n = s.n;
+    if (!tiled) {
+        k_direct_global<kMethod, kQuirk, kEpsZero><<<(n + 255) / 256, 256, 0, st>>>(s, p, eps);
+        return cudaGetLastError();
+    }
+    // pick bodies per thread so the i-blocks fill the GPU, split j otherwise
+    const int want = sm_count * 2;
+    int bx4 = (n + kDirectThreads * 4 - 1) / (kDirectThreads * 4);
+    int bx2 = (n + kDirectThreads * 2 - 1) / (kDirectThreads * 2);
+    int bx1 = (n + kDirectThreads - 1) / kDirectThreads;
+    const int ntiles = (n + kTile - 1) / kTile;
+    if (bx4 >= want) {
+        k_direct_tiled<4, kMethod, kQuirk, kEpsZero><<<dim3(bx4, 1), kDirectThreads, 0, st>>>(s, p, eps, part);
+        return cudaGetLastError();
+    }
+    if (bx2 >= want) {
+        k_direct_tiled<2, kMethod, kQuirk, kEpsZero><<<dim3(bx2, 1), kDirectThreads, 0, st>>>(s, p, eps, part);
+        return cudaGetLastError();
+    }
+    int split = (want + bx1 - 1) / bx1;
+    if (split > ntiles) split = ntiles;
+    if (split < 1) split = 1;
+    if (split == 1) {
+        k_direct_tiled<1, kMethod, kQuirk, kEpsZero><<<dim3(bx1, 1), kDirectThreads, 0, st>>>(s, p, eps, part);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaMemsetAsync(part, 0, sizeof(float4) * (size_t)n, st);
+    if (e != cudaSuccess) return e;
+    k_direct_tiled<1, kMethod, kQuirk, kEpsZero><<<dim3(bx1, split), kDirectThreads, 0, st>>>(s, p, eps, part);
+    k_integrate_partial<kMethod><<<(n + 255) / 256, 256, 0, st>>>(s, p, part);
+    return cudaGetLastError();
+}
+
+template <int kMethod>
+static cudaError_t launch_direct_m(const DevSim &s, const StepParams &p, float eps, int tiled, int quirk,
+                                   int sm_count, cudaStream_t st, float4 *part) {
+    const bool ez = !(eps > 0.0f);
+    if (quirk) return launch_direct_t<kMethod, true, false>(s, p, eps, tiled, sm_count, st, part);
+    if (ez) return launch_direct_t<kMethod, false, true>(s, p, eps, tiled, sm_count, st, part);
+    return launch_direct_t<kMethod, false, false>(s, p, eps, tiled, sm_count, st, part);
+}
+
+// `p.eps` is the softening to use; s.part (N float4) holds the partial sums
+// of a split j range.
+cudaError_t launch_direct(const DevSim &s, const StepParams &p, int tiled, int quirk, int sm_count,
+                          cudaStream_t st) {
+    float4 *part = s.part;
+    switch (p.method) {
+    case 1: return launch_direct_m<1>(s, p, p.eps, tiled, quirk, sm_count, st, part);
+    case 2: return launch_direct_m<2>(s, p, p.eps, tiled, quirk, sm_count, st, part);
+    case 3: return launch_direct_m<3>(s, p, p.eps, tiled, quirk, sm_count, st, part);
+    default: return launch_direct_m<0>(s, p, p.eps, tiled, quirk, sm_count, st, part);
+    }
+}
+
+cudaError_t launch_collision(const DevSim &s, int sm_count, cudaStream_t st) {
+    (void)sm_count;
+    k_collision<<<(s.n + kDirectThreads - 1) / kDirectThreads, kDirectThreads, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_vertices(const float4 *body, int n, float4 *dst, cudaStream_t st) {
+    k_copy_vertices<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(body, n, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack(const float *pos3, const float *mass, const float *vel3, float4 *body, float4 *vel,
+                        float4 *acc, int n, cudaStream_t st) {
+    const int blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+    k_pack<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(pos3, mass, vel3, body, vel, acc, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const float4 *body, const float4 *vel, const float4 *acc, float *pos3, float *vel3,
+                          float *acc3, int n, cudaStream_t st) {
+    const int blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+    k_unpack<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(body, vel, acc, pos3, vel3, acc3, n);
+    return cudaGetLastError();
+}
+
+}  // namespace nbgb

@@ -1,0 +1,444 @@
+// k_tree.cu -- bounding box, octree build, centre-of-mass summarisation and
+// in-order sort of the Barnes-Hut step.
+//
+// Reference stages: boundary_reduce (kernels/boundary_reduce.cl), init
+// (kernels/init.cl), build_tree (kernels/build_tree.cl, build_tree.hcl),
+// saturate_tree (kernels/saturate_tree.cl) and the empty sort
+// (kernels/sort.cl).  Each is re-designed for sm_103a; the differences that
+// change results are listed at each kernel.
+#include <cooperative_groups.h>
+
+#include "nbgb_internal.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace nbgb {
+
+// ---------------------------------------------------------------------------
+// reset: the per-step part of init (kernels/init.cl:26-33).  The reference
+// also rewrites every child slot of every node (init.cl:17-19, 32 B per node
+// and step); here a cell's eight slots are cleared by the thread that
+// allocates it, so only the root needs it.  The status word is cleared by the
+// host once per nb_step call, so an error stays visible to the later steps.
+// ---------------------------------------------------------------------------
+__global__ void k_reset(DevSim s) {
+    Ctrl *c = s.ctrl;
+    const int t = threadIdx.x;
+    if (t < 3) c->bbox_key[t] = 0xFFFFFFFFu;
+    else if (t < 6) c->bbox_key[t] = 0u;
+    if (t < 8) s.child[s.cap * 8 + t] = kEmpty;
+    if (t == 0) {
+        c->bottom = s.n + s.cap;
+        c->max_depth = 0;
+        c->work = 0;
+        s.arrive[s.cap] = 0;
+        s.start[s.cap] = 0;
+        s.count[s.cap] = 0;
+        s.parent[s.cap] = -1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// bbox: exact component-wise min/max over all bodies.  The reference's
+// two-kernel reduction samples only 2*WG bodies as wired (the host passes
+// the position buffer to parallel_reduce_root, src/MyApp.cpp:282); this is
+// the true reduction.  Floats are reduced as order-preserving integer keys
+// (IMNMX, exact, -0 < +0), warp shuffles, then one atomic per component per
+// block.  HBM-bound: 16 B read per body.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_bbox(const float4 *__restrict__ b, int n, Ctrl *c) {
+    unsigned mn0 = 0xFFFFFFFFu, mn1 = 0xFFFFFFFFu, mn2 = 0xFFFFFFFFu, mx0 = 0u, mx1 = 0u, mx2 = 0u;
+    int bad = -1;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float4 p = __ldg(&b[i]);
+        if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) bad = i;
+        const unsigned kx = f2key(p.x), ky = f2key(p.y), kz = f2key(p.z);
+        mn0 = min(mn0, kx); mx0 = max(mx0, kx);
+        mn1 = min(mn1, ky); mx1 = max(mx1, ky);
+        mn2 = min(mn2, kz); mx2 = max(mx2, kz);
+    }
+    mn0 = __reduce_min_sync(0xffffffffu, mn0);
+    mn1 = __reduce_min_sync(0xffffffffu, mn1);
+    mn2 = __reduce_min_sync(0xffffffffu, mn2);
+    mx0 = __reduce_max_sync(0xffffffffu, mx0);
+    mx1 = __reduce_max_sync(0xffffffffu, mx1);
+    mx2 = __reduce_max_sync(0xffffffffu, mx2);
+    __shared__ unsigned red[8][6];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        red[w][0] = mn0; red[w][1] = mn1; red[w][2] = mn2;
+        red[w][3] = mx0; red[w][4] = mx1; red[w][5] = mx2;
+    }
+    if (bad >= 0) set_status(c, kStNonFinite, bad);
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        unsigned v = red[0][k];
+        const int nw = blockDim.x >> 5;
+        for (int j = 1; j < nw; ++j) v = k < 3 ? min(v, red[j][k]) : max(v, red[j][k]);
+        if (k < 3) atomicMin(&c->bbox_key[k], v);
+        else atomicMax(&c->bbox_key[k], v);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Geometry of the build.  Both policies keep `g` = the region of the slot the
+// body is about to enter, so the split can give a new cell that region.
+// ---------------------------------------------------------------------------
+struct GeoCube {  // Burtscher: cubic root, child centre = centre -/+ r/2
+    float cx, cy, cz, r;
+    __device__ __forceinline__ int octant(float x, float y, float z) const {
+        return (y < cy ? 4 : 0) + (x < cx ? 2 : 0) + (z < cz ? 1 : 0);
+    }
+    __device__ __forceinline__ void descend(float x, float y, float z) {
+        r = __fmul_rn(r, 0.5f);
+        cx = __fadd_rn(cx, x < cx ? -r : r);
+        cy = __fadd_rn(cy, y < cy ? -r : r);
+        cz = __fadd_rn(cz, z < cz ? -r : r);
+    }
+};
+
+struct RefBox {  // the reference: calculateOctantIdx / adjustBoundaryValues
+    float mnx, mny, mnz, mxx, mxy, mxz;
+    // build_tree.hcl:14-29 -- 4*(dy<0) + 2*(dx<0) + (dz<0), centre (max+min)/2
+    __device__ __forceinline__ int octant(float x, float y, float z) const {
+        const float cx = __fmul_rn(__fadd_rn(mxx, mnx), 0.5f);
+        const float cy = __fmul_rn(__fadd_rn(mxy, mny), 0.5f);
+        const float cz = __fmul_rn(__fadd_rn(mxz, mnz), 0.5f);
+        return (y < cy ? 4 : 0) + (x < cx ? 2 : 0) + (z < cz ? 1 : 0);
+    }
+    // build_tree.hcl:31-54, y bounds following the x difference (:42-46)
+    __device__ __forceinline__ void descend(float x, float y, float z) {
+        const float cx = __fmul_rn(__fadd_rn(mxx, mnx), 0.5f);
+        const float cy = __fmul_rn(__fadd_rn(mxy, mny), 0.5f);
+        const float cz = __fmul_rn(__fadd_rn(mxz, mnz), 0.5f);
+        if (x > cx) mnx = cx; else mxx = cx;
+        if (x > cx) mny = cy; else mxy = cy;
+        if (z > cz) mnz = cz; else mxz = cz;
+        (void)y;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// build: concurrent octree insertion with atomicCAS child locks (Burtscher;
+// kernels/build_tree.cl:42-161).  Empty slot: CAS(-1 -> body).  Slot holding
+// a body: CAS(body -> LOCKED), grow a chain of cells until the two bodies
+// separate, publish the chain with one release store of its top cell.
+// Cells come from one downward counter with warp-aggregated atomicSub (one
+// atomic per converged group of splitting threads).  A fresh cell's eight
+// slots, parent link, arrival counter and sort start are initialised by the
+// allocating thread before publication.  Every retry loop is bounded
+// (kSpinCap) and watches the status word; a cell overflow or an over-deep
+// chain restores the locked slot, records the status and leaves.
+//
+// Reference semantics (kRef): the first probe is slot 0 of the super-root
+// without an octant test (build_tree.cl:57-65); the root region is the
+// bounding box; boxes halve as adjustBoundaryValues does.
+// ---------------------------------------------------------------------------
+template <class Geo, bool kRef>
+__global__ void __launch_bounds__(256) k_build(DevSim s) {
+    Ctrl *ctrl = s.ctrl;
+    if (read_status(ctrl)) return;
+    const int n = s.n, root = n + s.cap;
+    float box[6];
+    load_box(ctrl, box);
+    Geo root_g;
+    if constexpr (kRef) {
+        root_g = Geo{box[0], box[1], box[2], box[3], box[4], box[5]};
+    } else {
+        const float ex = box[3] - box[0], ey = box[4] - box[1], ez = box[5] - box[2];
+        float m = ex > ey ? ex : ey;
+        m = m > ez ? m : ez;
+        root_g = Geo{__fmul_rn(__fadd_rn(box[0], box[3]), 0.5f), __fmul_rn(__fadd_rn(box[1], box[4]), 0.5f),
+                     __fmul_rn(__fadd_rn(box[2], box[5]), 0.5f), __fmul_rn(0.5f, m)};
+    }
+    int local_max = 0;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float4 P = s.body_cur[i];
+        Geo g = root_g;
+        int node = root, slot, depth = 0;
+        if constexpr (kRef) {
+            slot = 0;
+        } else {
+            slot = g.octant(P.x, P.y, P.z);
+            g.descend(P.x, P.y, P.z);
+        }
+        int *cslot = &s.child[(node - n) * 8 + slot];
+        int ch = ld_volatile(cslot);
+        long long spins = 0;
+        while (true) {
+            while (ch >= n) {  // descend through published cells
+                node = ch;
+                slot = g.octant(P.x, P.y, P.z);
+                g.descend(P.x, P.y, P.z);
+                ++depth;
+                cslot = &s.child[(node - n) * 8 + slot];
+                ch = ld_volatile(cslot);
+            }
+            if (ch == kEmpty) {
+                if (atomicCAS(cslot, kEmpty, i) == kEmpty) break;
+            } else if (ch >= 0) {
+                if (atomicCAS(cslot, ch, kLocked) == ch) {
+                    const int og = ch;
+                    const float4 O = s.body_cur[og];
+                    Geo og_g = g;
+                    int patch = -1, link_node = node, link_slot = slot, c2;
+                    int fail = 0;
+                    do {
+                        cg::coalesced_group grp = cg::coalesced_threads();
+                        int base = 0;
+                        if (grp.thread_rank() == 0) base = atomicSub(&ctrl->bottom, (int)grp.size());
+                        base = grp.shfl(base, 0);
+                        const int cell = base - 1 - (int)grp.thread_rank();
+                        ++depth;
+                        if (cell < n) { fail = kStCellOverflow; break; }
+                        if (depth > 2 * kMaxDepth) { fail = kStDepth; break; }
+                        patch = max(patch, cell);
+                        const int c = cell - n;
+                        int4 *row = reinterpret_cast<int4 *>(&s.child[c * 8]);
+                        row[0] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+                        row[1] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+                        s.parent[c] = link_node;
+                        s.arrive[c] = 0;
+                        s.start[c] = -1;
+                        if (patch != cell) s.child[(link_node - n) * 8 + link_slot] = cell;
+                        const int oslot = og_g.octant(O.x, O.y, O.z);
+                        og_g.descend(O.x, O.y, O.z);
+                        s.child[c * 8 + oslot] = og;
+                        slot = g.octant(P.x, P.y, P.z);
+                        g.descend(P.x, P.y, P.z);
+                        link_node = cell;
+                        link_slot = slot;
+                        c2 = (slot == oslot) ? og : kEmpty;
+                    } while (c2 >= 0);
+                    if (fail) {
+                        st_volatile(cslot, og);  // release the lock unchanged
+                        set_status(ctrl, fail, i);
+                        return;
+                    }
+                    s.child[(link_node - n) * 8 + link_slot] = i;
+                    __threadfence();
+                    st_volatile(cslot, patch);  // publish the chain
+                    break;
+                }
+            }
+            if (++spins > kSpinCap) {
+                set_status(ctrl, kStSpinTimeout, i);
+                return;
+            }
+            if ((spins & 1023) == 0 && read_status(ctrl)) return;
+            ch = ld_volatile(cslot);
+        }
+        local_max = max(local_max, depth);
+    }
+    const unsigned am = __activemask();
+    const int wmax = __reduce_max_sync(am, local_max);
+    if ((threadIdx.x & 31) == __ffs(am) - 1) atomicMax(&ctrl->max_depth, wmax);
+}
+
+__device__ __forceinline__ void load_children(const int *child, int c, int chs[8], int &nch, int &nbody, int n) {
+    const int4 a0 = *reinterpret_cast<const int4 *>(&child[c * 8]);
+    const int4 a1 = *reinterpret_cast<const int4 *>(&child[c * 8 + 4]);
+    chs[0] = a0.x; chs[1] = a0.y; chs[2] = a0.z; chs[3] = a0.w;
+    chs[4] = a1.x; chs[5] = a1.y; chs[6] = a1.z; chs[7] = a1.w;
+    nch = 0;
+    nbody = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        nch += chs[j] >= 0;
+        nbody += (chs[j] >= 0) & (chs[j] < n);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// summarize: bottom-up centre of mass with L2-resident arrival counters.  One
+// thread per cell adds the number of the cell's body children to the cell's
+// counter in one atomic; a completed child cell adds one.  Whoever brings the
+// counter to the number of children computes the cell and then arrives at
+// the parent, and so on up to the root.  No thread ever waits, so no
+// co-residency of the grid is needed (saturate_tree.cl spins on child
+// masses, :96-117).  The completing thread sums the children in slot order
+// -- mass += m, centre += x*m, centre *= 1/mass, each rounded separately
+// (saturate_tree.cl:84-87,129-133) -- so the result does not depend on the
+// schedule and matches the oracle bit for bit.  It also writes the compacted
+// child list and the packed child {x,y,z,m} line the force walk reads (the
+// reference compacts in place, saturate_tree.cl:57-63, and skips the move
+// when a child's index equals its new slot number; that defect is not
+// reproduced).  Fences: release before every counter update, acquire after
+// the update that completes a cell; child-cell data written in this kernel is
+// read through L2 (__ldcg).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_summarize(DevSim s) {
+    if (read_status(s.ctrl)) return;
+    const int n = s.n, root = n + s.cap;
+    const int bottom = s.ctrl->bottom;
+    const int stride = gridDim.x * blockDim.x;
+    for (int k = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); k <= root; k += stride) {
+        int node = k;
+        int chs[8], nch, nbody;
+        load_children(s.child, node - n, chs, nch, nbody, n);
+        if (nbody == 0) continue;  // completed by its child cells
+        if (nbody != nch) {
+            const int old = atomicAdd(&s.arrive[node - n], nbody);
+            if (old + nbody != nch) continue;
+            __threadfence();
+        }
+        while (true) {
+            const int c = node - n;
+            float M = 0.0f, cx = 0.0f, cy = 0.0f, cz = 0.0f;
+            int cnt = 0, w = 0;
+            int wc[8];
+            float4 wp[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                wc[j] = kEmpty;
+                wp[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int ch = chs[j];
+                if (ch < 0) continue;
+                float4 pm;
+                int cc;
+                if (ch < n) {
+                    pm = s.body_cur[ch];
+                    cc = 1;
+                } else {
+                    pm = __ldcg(&s.cell_pm[ch - n]);
+                    cc = __ldcg(&s.count[ch - n]);
+                }
+                M = __fadd_rn(M, pm.w);
+                cx = __fadd_rn(cx, __fmul_rn(pm.x, pm.w));
+                cy = __fadd_rn(cy, __fmul_rn(pm.y, pm.w));
+                cz = __fadd_rn(cz, __fmul_rn(pm.z, pm.w));
+                cnt += cc;
+                // w <= j, so a static index write through a select chain
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (q == w) { wc[q] = ch; wp[q] = pm; }
+                ++w;
+            }
+            int4 *wrow = reinterpret_cast<int4 *>(&s.wchild[c * 8]);
+            wrow[0] = make_int4(wc[0], wc[1], wc[2], wc[3]);
+            wrow[1] = make_int4(wc[4], wc[5], wc[6], wc[7]);
+            float4 *prow = &s.wpm[c * 8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) prow[q] = wp[q];
+            const float inv = __frcp_rn(M);
+            s.count[c] = cnt;
+            s.cell_pm[c] = make_float4(__fmul_rn(cx, inv), __fmul_rn(cy, inv), __fmul_rn(cz, inv), M);
+            if (node == root) break;
+            const int p = s.parent[c];
+            load_children(s.child, p - n, chs, nch, nbody, n);
+            __threadfence();
+            const int old = atomicAdd(&s.arrive[p - n], 1);
+            if (old + 1 != nch) break;
+            __threadfence();
+            node = p;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// sort: in-order body placement from subtree counts (Burtscher's sort; the
+// reference's kernels/sort.cl is empty).  Cells are visited from the root
+// downward (descending index: a parent was allocated before its children);
+// a cell waits -- bounded -- until its parent has published its start, then
+// hands each child cell a start (running sum of counts in slot order) and
+// places each child body.  The result is the depth-first listing of bodies
+// in slot order, which the oracle's orc_sort reproduces exactly.  Launched
+// on a grid no larger than what is co-resident.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_sort(DevSim s) {
+    Ctrl *ctrl = s.ctrl;
+    if (read_status(ctrl)) return;
+    const int n = s.n, root = n + s.cap;
+    const int bottom = ctrl->bottom;
+    const int stride = gridDim.x * blockDim.x;
+    for (int k = root - (int)(blockIdx.x * blockDim.x + threadIdx.x); k >= bottom; k -= stride) {
+        const int c = k - n;
+        int st = ld_volatile(&s.start[c]);
+        long long spins = 0;
+        while (st < 0) {
+            if (++spins > kSpinCap) {
+                set_status(ctrl, kStSpinTimeout, k);
+                return;
+            }
+            if ((spins & 1023) == 0 && read_status(ctrl)) return;
+            __nanosleep(32);
+            st = ld_volatile(&s.start[c]);
+        }
+        const int4 a0 = *reinterpret_cast<const int4 *>(&s.wchild[c * 8]);
+        const int4 a1 = *reinterpret_cast<const int4 *>(&s.wchild[c * 8 + 4]);
+        const int chs[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int ch = chs[j];
+            if (ch < 0) break;
+            if (ch >= n) {
+                st_volatile(&s.start[ch - n], st);
+                st += s.count[ch - n];
+            } else {
+                if ((unsigned)st >= (unsigned)n) {  // inconsistent counts: never write past sorted[]
+                    set_status(ctrl, kStSpinTimeout, st);
+                    return;
+                }
+                s.sorted[st] = ch;
+                ++st;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static int resident_blocks(const void *fn, int threads, int sm_count) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * sm_count;
+}
+
+cudaError_t launch_reset(const DevSim &s, cudaStream_t st) {
+    k_reset<<<1, 32, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bbox(const DevSim &s, int sm_count, cudaStream_t st) {
+    int blocks = sm_count * 4;
+    const int need = (s.n + 255) / 256;
+    if (blocks > need) blocks = need > 0 ? need : 1;
+    k_bbox<<<blocks, 256, 0, st>>>(s.body_cur, s.n, s.ctrl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build(const DevSim &s, int tree_ref, int sm_count, cudaStream_t st) {
+    const void *fn = tree_ref ? (const void *)k_build<RefBox, true> : (const void *)k_build<GeoCube, false>;
+    int blocks = resident_blocks(fn, 256, sm_count);
+    const int need = (s.n + 255) / 256;
+    if (blocks > need) blocks = need > 0 ? need : 1;
+    if (tree_ref) k_build<RefBox, true><<<blocks, 256, 0, st>>>(s);
+    else k_build<GeoCube, false><<<blocks, 256, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_summarize(const DevSim &s, int sm_count, cudaStream_t st) {
+    int blocks = sm_count * 8;
+    const int need = (s.cap + 1 + 255) / 256;
+    if (blocks > need) blocks = need > 0 ? need : 1;
+    k_summarize<<<blocks, 256, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort(const DevSim &s, int sm_count, cudaStream_t st) {
+    int blocks = resident_blocks((const void *)k_sort, 256, sm_count);
+    const int need = (s.cap + 1 + 255) / 256;
+    if (blocks > need) blocks = need;
+    k_sort<<<blocks, 256, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+}  // namespace nbgb

@@ -1,0 +1,149 @@
+// nbgb_internal.cuh -- device data layout and helpers shared by the kernels.
+//
+// Layout in HBM (one system of N bodies, C cells):
+//   body_pm[2][N]  float4 {x,y,z,m}     positions double-buffered per step
+//   vel[N], acc[N] float4               velocity / last acceleration (w unused)
+//   node index space: bodies [0,N), cells [N, N+C), root N+C (the
+//   reference's index space, src/MyApp.cpp:71-83); cell arrays are indexed
+//   by cell - N and have C+1 entries (the root is the last one).
+//   child[(C+1)*8]   int   octant slots written by the build
+//   wchild[(C+1)*8]  int   the same children compacted in slot order
+//   wpm[(C+1)*8]     float4 {x,y,z,m} of those children, packed per cell so
+//                    the force walk reads one 128-byte line per opened cell
+//   cell_pm[C+1]     float4 centre of mass + mass
+//   count/start/arrive/parent[C+1] int (parent: of a cell), sorted[N] int
+//   Ctrl             bbox keys, allocation counter, max depth, status
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nbgb {
+
+constexpr int kMaxDepth = 64;
+constexpr int kLocked = -2;
+constexpr int kEmpty = -1;
+
+// device status codes (same values as nb_status)
+constexpr int kStOk = 0;
+constexpr int kStCellOverflow = 4;
+constexpr int kStDepth = 5;
+constexpr int kStSpinTimeout = 6;
+constexpr int kStNonFinite = 7;
+
+// bounded waits: iterations before a device wait gives up with kStSpinTimeout
+constexpr long long kSpinCap = 1LL << 24;
+
+struct Ctrl {
+    unsigned bbox_key[6];  // order-preserving keys: min xyz, max xyz
+    int bottom;            // lowest allocated cell index
+    int max_depth;
+    int work;              // dynamic work counter of the force pass
+    int pad0;
+    // cleared by the host once per nb_step call (everything from here on)
+    int status;
+    int status_info;
+    unsigned long long interactions;  // body-node interactions of the force passes
+    unsigned long long opened;        // cells opened by the force passes
+};
+
+struct DevSim {
+    int n;
+    int cap;
+    const float4 *body_cur;
+    float4 *body_next;
+    float4 *vel;
+    float4 *acc;
+    int *parent;
+    int *child;
+    int *wchild;
+    float4 *wpm;
+    float4 *cell_pm;
+    int *count;
+    int *start;
+    int *arrive;
+    int *sorted;
+    float4 *part;  // N partial accelerations of a split direct sum
+    Ctrl *ctrl;
+};
+
+struct StepParams {
+    float dt;
+    float G;
+    float theta;
+    float eps;
+    int method;      // 1 leapfrog as written, 2 euler, 3 kdk
+    int kdk_primed;
+    int tree_ref;    // reference tree semantics
+    int crit_ref;    // reference opening thresholds
+};
+
+__device__ __forceinline__ unsigned f2key(float f) {
+    unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key2f(unsigned k) {
+    unsigned b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(b);
+}
+
+__device__ __forceinline__ void set_status(Ctrl *c, int code, int info) {
+    if (atomicCAS(&c->status, 0, code) == 0) c->status_info = info;
+}
+__device__ __forceinline__ int read_status(const Ctrl *c) {
+    return *(volatile const int *)&c->status;
+}
+
+__device__ __forceinline__ int ld_volatile(const int *p) { return *(volatile const int *)p; }
+__device__ __forceinline__ void st_volatile(int *p, int v) { *(volatile int *)p = v; }
+
+// Opening thresholds per depth, as in the oracle's orc_bh_thresholds.
+__device__ __forceinline__ void make_thresholds(const float box[6], float theta, float eps, int crit_ref,
+                                                float *dq) {
+    float radius = 0.5f * fmaxf(fmaxf(box[3] - box[0], box[4] - box[1]), box[5] - box[2]);
+    float d0;
+    if (crit_ref) {
+        d0 = theta > 0.0f ? __fdiv_rn(__fmul_rn(radius, radius), theta) : __fmul_rn(radius, radius);
+    } else {
+        float itolsq = __fdiv_rn(1.0f, __fmul_rn(theta, theta));
+        d0 = __fmul_rn(__fmul_rn(radius, radius), itolsq);
+    }
+    float add = crit_ref ? eps : __fmul_rn(eps, eps);
+    float base = d0;
+    for (int i = 0; i < kMaxDepth; ++i) {
+        dq[i] = __fadd_rn(base, add);
+        base = __fmul_rn(0.25f, base);
+    }
+}
+
+__device__ __forceinline__ void load_box(const Ctrl *c, float box[6]) {
+    for (int k = 0; k < 6; ++k) box[k] = key2f(c->bbox_key[k]);
+}
+
+// Launch helpers implemented in the kernel translation units.
+struct LaunchShape {
+    int blocks;
+    int threads;
+};
+
+cudaError_t launch_reset(const DevSim &s, cudaStream_t st);
+cudaError_t launch_bbox(const DevSim &s, int sm_count, cudaStream_t st);
+cudaError_t launch_build(const DevSim &s, int tree_ref, int sm_count, cudaStream_t st);
+cudaError_t launch_summarize(const DevSim &s, int sm_count, cudaStream_t st);
+cudaError_t launch_sort(const DevSim &s, int sm_count, cudaStream_t st);
+cudaError_t launch_force(const DevSim &s, const StepParams &p, int compensated, int sm_count, cudaStream_t st);
+cudaError_t launch_direct(const DevSim &s, const StepParams &p, int tiled, int quirk, int sm_count,
+                          cudaStream_t st);
+cudaError_t launch_collision(const DevSim &s, int sm_count, cudaStream_t st);
+cudaError_t launch_copy_vertices(const float4 *body, int n, float4 *dst, cudaStream_t st);
+cudaError_t launch_pack(const float *pos3, const float *mass, const float *vel3, float4 *body, float4 *vel,
+                        float4 *acc, int n, cudaStream_t st);
+cudaError_t launch_unpack(const float4 *body, const float4 *vel, const float4 *acc, float *pos3, float *vel3,
+                          float *acc3, int n, cudaStream_t st);
+cudaError_t launch_export_tree(const DevSim &s, int *children_full, float *pos_full, float *mass_full,
+                               int *count_full, cudaStream_t st);
+cudaError_t launch_force_probe(const float4 *body, int n, const int *sample, int ns, double eps, double G,
+                               double *out3, cudaStream_t st);
+cudaError_t launch_diagnostics(const float4 *body, const float4 *vel, int n, int with_potential, double eps,
+                               double G, double *out9, cudaStream_t st);
+
+}  // namespace nbgb

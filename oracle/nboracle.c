@@ -412,7 +412,8 @@ void orc_bh_thresholds(int criterion, const float box6[6], float theta, float ep
  * child cell is accumulated when EVERY body of the group has
  * d2 >= dq[depth] (work_group_all, :121) and pushed otherwise; an empty
  * slot pops (:140-142).  Groups are consecutive entries of `order`
- * (identity when NULL, i.e. the reference's g_id order).
+ * (identity when NULL, i.e. the reference's g_id order); only the first
+ * `norder` entries of `order` are walked (a sample of groups).
  *
  * arith == ORC_ARITH_REFERENCE: d2 = eps*eps + dx*dx + dy*dy + dz*dz,
  *   F = m*r*r*r with r = 1/sqrt(d2), acc += diff*F (:117-128).
@@ -423,15 +424,17 @@ void orc_bh_thresholds(int criterion, const float box6[6], float theta, float ep
  * compensated: per-component TwoSum accumulation (acc = hi + lo).
  * acc3 receives G*acc.  Returns 0, or ORC_ERR_DEPTH on stack overflow. */
 int orc_bh_force(const float *node_pos, const float *node_mass, const int *children, int n, int nodes,
-                 const float *dq, float eps, float G, int arith, int vote_width, const int *order,
+                 const float *dq, float eps, float G, int arith, int vote_width, const int *order, int norder,
                  int skip_self, int compensated, float *acc3) {
     const int root = n + nodes;
-    const int ngroups = (n + vote_width - 1) / vote_width;
+    if (vote_width < 1 || vote_width > 64) return ORC_ERR_ARG;
+    if (!order || norder <= 0 || norder > n) norder = n;
+    const int ngroups = (norder + vote_width - 1) / vote_width;
     const float eps2 = eps * eps;
     int err = 0;
 #pragma omp parallel for schedule(dynamic, 4)
     for (int g = 0; g < ngroups; ++g) {
-        int lanes = n - g * vote_width;
+        int lanes = norder - g * vote_width;
         if (lanes > vote_width) lanes = vote_width;
         int body[64];
         float px[64], py[64], pz[64];

@@ -47,7 +47,7 @@ def lib():
             "orc_saturate": ([i, i, i, i, P, P, P, P], i),
             "orc_sort": ([P, i, i, P], i),
             "orc_bh_thresholds": ([i, P, f, f, i, P], None),
-            "orc_bh_force": ([P, P, P, i, i, P, f, f, i, i, P, i, i, P], i),
+            "orc_bh_force": ([P, P, P, i, i, P, f, f, i, i, P, i, i, i, P], i),
             "orc_direct_fp32": ([P, P, i, f, f, i, i, P], None),
             "orc_direct_fp64": ([P, P, i, d, d, P, i, P], None),
             "orc_direct_quirk_global": ([P, P, i, f, P], None),
@@ -170,10 +170,13 @@ def thresholds(criterion, box6, theta, eps, max_depth):
 
 def bh_force(t: Tree, dq, eps, G, arith=ARITH_FMA, vote_width=32, order=None, skip_self=True,
              compensated=False):
+    """Forces for the bodies of `order` (all bodies when None), walked in
+    groups of `vote_width` consecutive entries."""
     acc = np.zeros(t.n * 3, np.float32)
     order = i32(order) if order is not None else None
+    norder = 0 if order is None else len(order)
     rc = lib().orc_bh_force(_p(t.pos), _p(t.mass), _p(t.children), t.n, t.nodes, _p(f32(dq)), eps, G, arith,
-                            vote_width, _p(order), 1 if skip_self else 0, 1 if compensated else 0, _p(acc))
+                            vote_width, _p(order), norder, 1 if skip_self else 0, 1 if compensated else 0, _p(acc))
     return acc.reshape(-1, 3), rc
 
 

@@ -1,0 +1,156 @@
+"""The C ABI without a GPU: the library builds for sm_103a, loads, exports
+every function include/nbgb.h declares, and its host-only entry points
+behave.  No compute call needs a device here."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "nbgb.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(nb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(nbgb_lib):
+    syms = subprocess.run(["nm", "-D", "--defined-only", nbgb_lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (nb_\w+)", syms))
+    declared = declared_functions()
+    assert declared, "no declarations parsed"
+    missing = [d for d in declared if d not in exported]
+    assert not missing, missing
+    # the Python binding covers the whole ABI as well
+    assert set(declared) == set(nbgb_lib.SIGNATURES)
+
+
+def test_binary_targets_sm103a(nbgb_lib):
+    out = subprocess.run(["cuobjdump", "--list-elf", nbgb_lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "sm_103a" in out
+
+
+def test_config_struct_layout_and_defaults(nbgb_lib):
+    nb = nbgb_lib
+    c = nb.default_config()
+    # SimulationConfig / BarnesHutConfig / Simulation defaults
+    # (src/SimulationConfig.h:85-104,131-132; src/BarnesHutConfig.h:58-60)
+    assert c.num_of_bodies == 20000
+    assert np.isclose(c.gravitational_constant, 6.67e-11)
+    assert c.starting_speed_mul == 1.0 and c.starting_volume_radius == 1.5
+    assert c.number_of_massive_objects == 0 and c.massive_object_mass == 1.0
+    assert c.collision == 0
+    assert c.pos_config == nb.UNIFORM_POS and c.vel_config == nb.FUNC_ZERO_VEL
+    assert c.algo_config == nb.BRUTE_FORCE_GLOBAL
+    assert c.mass_mean == 0.5 and c.mass_deviation == 0.25
+    assert c.numerical_method == nb.EULER
+    assert c.max_octree_depth == 32 and c.theta == 1.5 and np.isclose(c.epsilon, 0.01)
+    assert c.simulation_speed_mul == 1.0 and np.isclose(c.particle_size, 0.05)
+
+
+def test_config_layout_matches_c_header(nbgb_lib, tmp_path):
+    """ctypes mirror == the C struct, field by field (gcc on include/nbgb.h)."""
+    nb = nbgb_lib
+    fields = [f for f, _ in nb.NbConfig._fields_]
+    src = ["#include <stdio.h>", "#include <stddef.h>", '#include "nbgb.h"', "int main(void){",
+           'printf("%zu\\n", sizeof(nb_config));']
+    src += [f'printf("%zu\\n", offsetof(nb_config, {f}));' for f in fields]
+    src += ["return 0;}"]
+    c_file = tmp_path / "layout.c"
+    c_file.write_text("\n".join(src))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(c_file), "-o", str(exe)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    assert vals[0] == ctypes.sizeof(nb.NbConfig)
+    for f, off in zip(fields, vals[1:]):
+        assert getattr(nb.NbConfig, f).offset == off, f
+
+
+def test_status_strings(nbgb_lib):
+    L = nbgb_lib.load()
+    assert L.nb_abi_version() == 1
+    for s in range(11):
+        assert L.nb_status_string(s)
+    assert L.nb_status_string(nbgb_lib.ERR_CELL_OVERFLOW) == b"tree cell capacity exceeded"
+
+
+def test_ic_generator_deterministic_and_shaped(nbgb_lib):
+    nb = nbgb_lib
+    c = nb.default_config(num_of_bodies=20000, pos_config=nb.BALL_POS, starting_volume_radius=1.0,
+                          mass_config=nb.MASS_EQUAL, vel_config=nb.CIRCULAR_Z_VEL, gravitational_constant=1.0, seed=7)
+    p1, v1, m1 = nb.generate_ic(c)
+    p2, v2, m2 = nb.generate_ic(c)
+    assert np.array_equal(p1, p2) and np.array_equal(v1, v2) and np.array_equal(m1, m2)
+    r = np.linalg.norm(p1, axis=1)
+    assert r.max() <= 1.0 + 1e-6
+    # uniform in the ball: P(r < 1/2) = 1/8
+    assert abs(np.mean(r < 0.5) - 0.125) < 0.01
+    assert np.allclose(m1, 1.0 / 20000)
+    # tangential about z with |v| = sqrt(G M(<r) / r) = r for the unit ball of mass 1
+    assert np.allclose(v1[:, 2], 0.0)
+    assert np.allclose(np.einsum("ij,ij->i", v1[:, :2], p1[:, :2]), 0.0, atol=1e-5)
+    assert np.allclose(np.linalg.norm(v1, axis=1), r, rtol=1e-4)
+    c.seed = 8
+    p3, _, _ = nb.generate_ic(c)
+    assert not np.array_equal(p1, p3)
+
+
+def test_ic_reference_modes(nbgb_lib):
+    nb = nbgb_lib
+    c = nb.default_config(num_of_bodies=5000, seed=1)  # reference defaults: normal(0,1.5), |N(.5,.25)| masses
+    p, v, m = nb.generate_ic(c)
+    assert abs(p.std() - 1.5) < 0.05
+    assert np.all(m >= 0) and abs(m.mean() - 0.5) < 0.02
+    assert np.all(v == np.float32(np.finfo(np.float32).eps))  # FUNC_ZERO_VEL
+    c.number_of_massive_objects = 3
+    c.massive_object_mass = 50.0
+    _, _, m = nb.generate_ic(c)
+    assert np.all(m[:3] == 50.0) and np.all(m[3:] != 50.0)
+    c.pos_config = nb.SPHERE_POS
+    p, _, _ = nb.generate_ic(c)
+    assert np.allclose(np.linalg.norm(p, axis=1), 1.5, rtol=1e-5)
+    c.vel_config = nb.TANGENT_XZ_VEL
+    p, v, _ = nb.generate_ic(c)
+    assert np.allclose(v[:, 1], 0.0) and np.allclose(v[:, 0], p[:, 2]) and np.allclose(v[:, 2], -p[:, 0])
+    c.vel_config = nb.STARTING_IN_VEL
+    p, v, _ = nb.generate_ic(c)
+    assert np.allclose(np.linalg.norm(v, axis=1), 1.0, rtol=1e-5)
+    assert np.all(np.einsum("ij,ij->i", v, p) < 0)
+    c.pos_config = nb.NORMAL_SIGMA_POS
+    c.pos_sigma[:] = [1.0, 1.0, 0.2]
+    c.mass_config = nb.MASS_LOGNORMAL
+    c.number_of_massive_objects = 0
+    p, _, m = nb.generate_ic(c)
+    assert abs(p[:, 2].std() - 0.2) < 0.01 and abs(p[:, 0].std() - 1.0) < 0.05
+    assert np.isclose(m.sum(), 1.0, rtol=1e-5)
+
+
+def test_create_without_device_fails_cleanly(nbgb_lib):
+    import ctypes as ct
+    try:
+        drv = ct.CDLL("libcuda.so.1")
+        cnt = ct.c_int(0)
+        if drv.cuInit(0) == 0 and drv.cuDeviceGetCount(ct.byref(cnt)) == 0 and cnt.value > 0:
+            import pytest
+            pytest.skip("a GPU is present")
+    except OSError:
+        pass
+    L = nbgb_lib.load()
+    c = nbgb_lib.default_config(num_of_bodies=16)
+    h = ct.c_void_p()
+    st = L.nb_create(ct.byref(c), ct.byref(h))
+    assert st in (nbgb_lib.ERR_NO_DEVICE, nbgb_lib.ERR_CUDA)
+    assert not h.value
+
+
+def test_invalid_arguments_without_device(nbgb_lib):
+    import ctypes as ct
+    L = nbgb_lib.load()
+    c = nbgb_lib.default_config(num_of_bodies=0)
+    h = ct.c_void_p()
+    assert L.nb_create(ct.byref(c), ct.byref(h)) == nbgb_lib.ERR_INVALID_ARGUMENT
+    assert L.nb_step(None, 0.001, 1) == nbgb_lib.ERR_INVALID_ARGUMENT
+    assert L.nb_destroy(None) == nbgb_lib.ERR_INVALID_ARGUMENT

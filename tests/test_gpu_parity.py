@@ -1,0 +1,298 @@
+"""Parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Bit-exact: bounding box, tree topology in canonical octant-path form, cell
+masses / centres of mass / body counts, the sort permutation, the opening
+thresholds, the collision update and copy_vertices.  Within tolerance (the
+GPU uses the MUFU rsqrt and a different summation order): accelerations and
+positions after k steps.  Tolerances are stated per test.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def ball(n, seed, r=1.0):
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p = d * (r * rng.random(n) ** (1 / 3))[:, None]
+    return p.astype(np.float32)
+
+
+def normal(n, seed, sigma=(1.0, 1.0, 1.0)):
+    rng = np.random.default_rng(seed)
+    return (rng.normal(size=(n, 3)) * np.asarray(sigma)).astype(np.float32)
+
+
+def masses(n, seed, kind="equal"):
+    if kind == "equal":
+        return np.full(n, 1.0 / n, np.float32)
+    rng = np.random.default_rng(seed + 1)
+    m = np.exp(0.5 * rng.normal(size=n))
+    return (m / m.sum()).astype(np.float32)
+
+
+def bh_sim(nb, pos, mass, theta, eps, G=1.0, tree=0, crit=0, method=2, precision=0, vel=None, cap=0):
+    sim = nb.Simulation(num_of_bodies=len(mass), algo_config=nb.BARNES_HUT, theta=theta, epsilon=eps,
+                        gravitational_constant=G, tree_semantics=tree, theta_semantics=crit,
+                        numerical_method=method, precision=precision, cell_capacity=cap)
+    sim.set_state(pos, mass, vel)
+    return sim
+
+
+def cell_table(children, mass, pos, count, n, root):
+    ch = children.reshape(-1, 8)
+    pos = pos.reshape(-1, 3)
+    out, stack = {}, [(root, ())]
+    while stack:
+        node, path = stack.pop()
+        out[path] = (mass[node], tuple(pos[node]), count[node])
+        for s in range(8):
+            c = ch[node][s]
+            if c >= n:
+                stack.append((c, path + (s,)))
+    return out
+
+
+def rel_to_typical(a, b):
+    """max |a_i - b_i| / rms |b|: error relative to the typical acceleration."""
+    scale = np.sqrt(np.mean(np.sum(b.astype(np.float64) ** 2, axis=1)))
+    return float(np.max(np.linalg.norm(a.astype(np.float64) - b, axis=1)) / scale)
+
+
+CASES = [
+    ("ball", 20000, 0.5, 0.01, 0, 0),
+    ("normal", 30000, 0.5, 0.005, 0, 0),
+    ("normal", 12345, 0.3, 0.005, 0, 0),
+    ("ball", 16384, 0.5, 0.01, 1, 1),   # the reference's tree and thresholds
+    ("normal", 9000, 1.5, 0.01, 1, 1),  # the reference's default theta
+]
+
+
+@pytest.mark.parametrize("kind,n,theta,eps,tree,crit", CASES)
+def test_bh_stages_against_oracle(gpu, oracle, kind, n, theta, eps, tree, crit):
+    nb = gpu
+    pos = ball(n, n) if kind == "ball" else normal(n, n, (1.0, 1.0, 0.2))
+    mass = masses(n, n, "equal" if kind == "ball" else "lognormal")
+    sim = bh_sim(nb, pos, mass, theta, eps, tree=tree, crit=crit)
+    sim.step(0.0, 1)  # dt = 0: forces only, positions unchanged
+    # 1. bounding box, bit-exact
+    box = sim.stage_debug(nb.DEBUG_BBOX)
+    assert np.array_equal(box, oracle.bbox_exact(pos))
+    info = sim.stage_debug(nb.DEBUG_TREE_INFO)
+    cap = int(info[1])
+    # 2. topology, bit-exact in canonical path form
+    sem = oracle.SEM_REFERENCE if tree else oracle.SEM_GEOMETRIC
+    t = oracle.tree_build(sem, pos, mass, box, cap)
+    assert t.status == 0
+    children = sim.stage_debug(nb.DEBUG_CHILDREN)
+    pg, dg, fg = oracle.tree_paths(children, n, n + cap)
+    po, do, fo = oracle.tree_paths(t.children, n, t.root)
+    assert fg == n and fo == n
+    assert np.array_equal(dg, do) and np.array_equal(pg, po)
+    assert int(info[3]) == t.max_depth
+    assert int(info[2]) == t.bottom  # the same number of cells
+    # 3. summarisation, bit-exact (children summed in slot order)
+    assert oracle.saturate(t) == 0
+    mg = sim.stage_debug(nb.DEBUG_NODE_MASS)
+    xg = sim.stage_debug(nb.DEBUG_NODE_POS)
+    cg = sim.stage_debug(nb.DEBUG_BODY_COUNT)
+    tg = cell_table(children, mg, xg, cg, n, n + cap)
+    to = cell_table(t.children, t.mass, t.pos, t.body_count, n, t.root)
+    assert tg.keys() == to.keys()
+    bad = [k for k in to if tg[k] != to[k]]
+    assert not bad, (len(bad), bad[:3])
+    assert cg[n + cap] == n
+    # 4. sort permutation, bit-exact
+    srt_o, k = oracle.sort_bodies(t.children, n, t.root)
+    srt_g = sim.stage_debug(nb.DEBUG_SORTED)
+    assert k == n
+    assert np.array_equal(srt_g, srt_o)
+    # 5. thresholds, bit-exact
+    crit_o = oracle.CRIT_REFERENCE if crit else oracle.CRIT_STANDARD
+    dq = oracle.thresholds(crit_o, box, theta, eps, t.max_depth)
+    assert np.array_equal(sim.stage_debug(nb.DEBUG_DQ), dq)
+    # 6. accelerations: same votes (warps of 32 in sort order), same d^2 arithmetic;
+    #    the GPU's rsqrt and summation order stay within 2e-5 of the typical |a|
+    acc_o, rc = oracle.bh_force(t, dq, eps, 1.0, arith=oracle.ARITH_FMA, vote_width=32, order=srt_o)
+    assert rc == 0
+    _, _, acc_g, _ = sim.get_state()
+    err = rel_to_typical(acc_g, acc_o)
+    assert err < 2e-5, err
+
+
+def test_bh_accuracy_vs_fp64(gpu, oracle):
+    """theta=0.5 standard criterion: RMS relative force error vs FP64 <= 1e-3;
+    the GPU FP64 probe agrees with the CPU FP64 oracle."""
+    nb = gpu
+    n = 65536
+    pos = normal(n, 5, (1.0, 1.0, 0.2))
+    mass = masses(n, 5, "lognormal")
+    sim = bh_sim(nb, pos, mass, 0.5, 0.005)
+    sim.step(0.0, 1)
+    sample = np.random.default_rng(0).choice(n, 2048, replace=False).astype(np.int32)
+    mx, rms, per = sim.force_error(sample)
+    assert rms <= 1e-3, rms
+    a64 = oracle.direct_fp64(pos, mass, 0.005, 1.0, targets=sample[:256])
+    _, _, acc_g, _ = sim.get_state()
+    e_cpu = np.linalg.norm(acc_g[sample[:256]] - a64, axis=1) / np.linalg.norm(a64, axis=1)
+    assert np.allclose(e_cpu, per[:256], rtol=1e-6, atol=1e-12)
+
+
+@pytest.mark.parametrize("algo,quirk,n", [(1, 0, 4096), (2, 0, 4096), (2, 0, 5000), (2, 0, 70000), (1, 1, 3000),
+                                          (2, 1, 3000), (1, 0, 1000)])
+def test_direct_against_oracle(gpu, oracle, algo, quirk, n):
+    nb = gpu
+    pos = normal(n, 100 + n)
+    mass = masses(n, n, "lognormal")
+    sim = nb.Simulation(num_of_bodies=n, algo_config=algo, force_law=quirk, epsilon=0.05,
+                        gravitational_constant=1.0)
+    sim.set_state(pos, mass)
+    sim.step(0.0, 1)
+    _, _, acc_g, _ = sim.get_state()
+    if quirk:
+        # the reference's arithmetic; the GPU visits every j once (no tile-0 reload)
+        acc_o = oracle.direct_quirk_global(pos, mass, 1.0) if algo == 1 else \
+            oracle.direct_quirk_local(pos, mass, 1.0, q12=False)
+    else:
+        acc_o = oracle.direct_fp32(pos, mass, 0.05, 1.0)
+    err = rel_to_typical(acc_g, acc_o)
+    assert err < 2e-5, err
+
+
+def test_direct_trajectory_config1(gpu, oracle):
+    """N=4096 normal(0,1), m=1/N, G=1, eps=0.05, dt=1e-3, 20 Euler steps of the
+    global direct sum: positions within 1e-5 (relative to their spread)."""
+    nb = gpu
+    n, steps, dt = 4096, 20, 1e-3
+    pos = normal(n, 0)
+    mass = masses(n, 0)
+    sim = nb.Simulation(num_of_bodies=n, algo_config=nb.BRUTE_FORCE_GLOBAL, epsilon=0.05, gravitational_constant=1.0)
+    sim.set_state(pos, mass)
+    sim.step(dt, steps)
+    pg, vg, _, _ = sim.get_state()
+    p, v, a = pos.copy(), np.zeros_like(pos), np.zeros_like(pos)
+    for _ in range(steps):
+        acc = oracle.direct_fp32(p, mass, 0.05, 1.0)
+        p, v, a = oracle.integrate(oracle.EULER, p, v, acc, a, dt)
+    assert np.max(np.abs(pg - p)) < 1e-5 * np.std(p)
+    assert np.max(np.abs(vg - v)) < 1e-4 * np.std(v)
+
+
+def test_bh_trajectory(gpu, oracle):
+    """BH (standard semantics), 5 Euler steps at N=16384: positions within 1e-5."""
+    nb = gpu
+    n, steps, dt, theta, eps = 16384, 5, 1e-3, 0.5, 0.01
+    pos = ball(n, 3)
+    mass = masses(n, 3)
+    sim = bh_sim(nb, pos, mass, theta, eps)
+    sim.step(dt, steps)
+    pg, _, _, _ = sim.get_state()
+    p, v, a = pos.copy(), np.zeros_like(pos), np.zeros_like(pos)
+    for _ in range(steps):
+        acc, _, _ = oracle.bh_step_forces(p, mass, theta, eps, 1.0)
+        p, v, a = oracle.integrate(oracle.EULER, p, v, acc, a, dt)
+    assert np.max(np.abs(pg - p)) < 1e-5 * np.std(p)
+
+
+@pytest.mark.parametrize("method", [1, 2, 3])
+def test_integrators(gpu, oracle, method):
+    nb = gpu
+    n, dt = 2048, 2e-3
+    pos = normal(n, 9)
+    mass = masses(n, 9)
+    vel = (np.random.default_rng(1).normal(size=(n, 3)) * 0.1).astype(np.float32)
+    sim = nb.Simulation(num_of_bodies=n, algo_config=nb.BRUTE_FORCE_LOCAL, epsilon=0.05, gravitational_constant=1.0,
+                        numerical_method=method)
+    sim.set_state(pos, mass, vel)
+    sim.step(dt, 2)
+    pg, vg, _, _ = sim.get_state()
+    p, v, a = pos.copy(), vel.copy(), np.zeros_like(pos)
+    for k in range(2):
+        acc = oracle.direct_fp32(p, mass, 0.05, 1.0)
+        p, v, a = oracle.integrate(method, p, v, acc, a, dt, primed=k > 0)
+    assert np.max(np.abs(pg - p)) < 1e-6 * np.std(p)
+    assert np.max(np.abs(vg - v)) < 1e-5 * np.std(v)
+
+
+def test_collision_bit_exact(gpu, oracle):
+    nb = gpu
+    n = 3000
+    pos = normal(n, 77, (0.05, 0.05, 0.05))
+    mass = masses(n, 77)
+    vel = (np.random.default_rng(2).normal(size=(n, 3)) * 0.1).astype(np.float32)
+    sim = nb.Simulation(num_of_bodies=n, algo_config=nb.BRUTE_FORCE_GLOBAL, collision=1, gravitational_constant=0.0)
+    sim.set_state(pos, mass, vel)
+    sim.step(0.0, 1)  # no gravity, no drift: the collision update alone
+    pg, vg, _, _ = sim.get_state()
+    assert np.array_equal(pg, pos)
+    vo = oracle.collision(pos, vel)
+    assert np.any(vo != vel)
+    assert np.array_equal(vg, vo)
+
+
+def test_copy_vertices(gpu, oracle):
+    nb = gpu
+    n = 1000
+    pos = normal(n, 4)
+    sim = nb.Simulation(num_of_bodies=n)
+    sim.set_state(pos, masses(n, 4))
+    assert np.array_equal(sim.copy_vertices(), oracle.copy_vertices(pos))
+
+
+def test_compensated_accumulation(gpu, oracle):
+    nb = gpu
+    n = 20000
+    pos = normal(n, 6, (1.0, 1.0, 0.2))
+    mass = masses(n, 6, "lognormal")
+    sim = bh_sim(nb, pos, mass, 0.5, 0.005, precision=nb.PRECISION_COMPENSATED)
+    sim.step(0.0, 1)
+    acc_o, t, srt = oracle.bh_step_forces(pos, mass, 0.5, 0.005, 1.0, compensated=True)
+    _, _, acc_g, _ = sim.get_state()
+    assert rel_to_typical(acc_g, acc_o) < 2e-5
+
+
+def test_update_clamps_frame_time(gpu):
+    nb = gpu
+    n = 512
+    pos = normal(n, 8)
+    mass = masses(n, 8)
+    a = nb.Simulation(num_of_bodies=n, gravitational_constant=1.0, simulation_speed_mul=2.0)
+    b = nb.Simulation(num_of_bodies=n, gravitational_constant=1.0, simulation_speed_mul=2.0)
+    a.set_state(pos, mass)
+    b.set_state(pos, mass)
+    a.update(1.0)          # clamped to 5e-3, times speed 2
+    b.step(0.01, 1)
+    assert np.array_equal(a.get_state()[0], b.get_state()[0])
+
+
+def test_cell_overflow_reports_and_keeps_state(gpu):
+    nb = gpu
+    n = 5000
+    pos = ball(n, 1)
+    mass = masses(n, 1)
+    sim = bh_sim(nb, pos, mass, 0.5, 0.01, cap=64)
+    st = sim.step(1e-3, 3, check=False)
+    assert st == nb.ERR_CELL_OVERFLOW
+    p, _, _, _ = sim.get_state()
+    assert np.array_equal(p, pos)
+
+
+def test_nonfinite_input_reported(gpu):
+    nb = gpu
+    n = 1000
+    pos = ball(n, 2)
+    pos[17, 1] = np.nan
+    sim = bh_sim(nb, pos, masses(n, 2), 0.5, 0.01)
+    assert sim.step(1e-3, 1, check=False) == nb.ERR_NONFINITE
+
+
+def test_coincident_bodies_do_not_hang(gpu):
+    nb = gpu
+    n = 1000
+    pos = ball(n, 3)
+    pos[5] = pos[6]
+    sim = bh_sim(nb, pos, masses(n, 3), 0.5, 0.01)
+    st = sim.step(1e-3, 1, check=False)
+    assert st in (nb.ERR_DEPTH, nb.ERR_CELL_OVERFLOW)
