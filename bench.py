@@ -38,7 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(name="bh_plummer_n4m_theta0.5", n=4194304, sigma=(1.0, 1.0, 0.2), mass_sigma=0.5, theta=0.5,
-                eps=0.005, dt=1e-3, G=1.0, precision="compensated")
+                eps=0.005, dt=1e-3, G=1.0, precision="compensated", multipole="quadrupole")
 PROBE_SAMPLES = 8192
 FP32_LANES_PER_SM = 128
 FLOPS_PER_INTERACTION = 12  # FP32-pipe instructions per interaction (3 sub, 3 fma, 3 mul, 3 fma)
@@ -176,7 +176,7 @@ def workload_ic(nb, n, seed):
 def make_sim(nb, n, precision, device):
     return nb.Simulation(num_of_bodies=n, algo_config=nb.BARNES_HUT, theta=WORKLOAD["theta"],
                          epsilon=WORKLOAD["eps"], gravitational_constant=WORKLOAD["G"], numerical_method=nb.EULER,
-                         precision=precision, device=device)
+                         precision=precision, device=device, multipole=nb.MULTIPOLE_QUADRUPOLE)
 
 
 # ---------------------------------------------------------------------------
@@ -195,6 +195,7 @@ def cpu_baseline(pos, mass, sample_groups=512, repeats=1):
         box = O.bbox_exact(pos)
         t = O.tree_build(O.SEM_GEOMETRIC, pos, mass, box, 2 * n)
         O.saturate(t)
+        quad = O.quadrupoles(t)
         srt, _ = O.sort_bodies(t.children, n, t.root)
         t1 = time.perf_counter()
         dq = O.thresholds(O.CRIT_STANDARD, box, WORKLOAD["theta"], WORKLOAD["eps"], t.max_depth)
@@ -203,7 +204,7 @@ def cpu_baseline(pos, mass, sample_groups=512, repeats=1):
         order = (pick[:, None] * 32 + np.arange(32)[None, :]).ravel()
         order = srt[order]
         t2 = time.perf_counter()
-        O.bh_force(t, dq, WORKLOAD["eps"], WORKLOAD["G"], vote_width=32, order=order, compensated=True)
+        O.bh_force(t, dq, WORKLOAD["eps"], WORKLOAD["G"], vote_width=32, order=order, compensated=True, quad=quad)
         t3 = time.perf_counter()
         step = (t1 - t0) + (t3 - t2) * (n / len(order))
         times.append(step)
@@ -225,7 +226,7 @@ def run_ours(args, dist: Dist):
     dist.barrier()
     import nbodysimulation_gb300 as nb
     L = nb.load()
-    n, dt = WORKLOAD["n"], WORKLOAD["dt"]
+    n, dt = args.n, WORKLOAD["dt"]
     dev = dist.local_rank
     pos, vel, mass = workload_ic(nb, n, seed=dist.rank)
     sim = make_sim(nb, n, nb.PRECISION_COMPENSATED, dev)
@@ -299,9 +300,9 @@ def run_ours(args, dist: Dist):
     force_ms = stage["force"]
     # algorithmic bytes of one force launch: per body sorted index 4 B, body
     # {x,y,z,m} 16 B, velocity 16 B read; body, velocity, acceleration 48 B
-    # written; per cell in the tree its child list 32 B and packed child line
-    # 128 B read once
-    alg_bytes = 84 * n + 160 * cells_used
+    # written; per cell in the tree its child list 32 B, packed child line
+    # 128 B and packed child quadrupoles 192 B read once
+    alg_bytes = 84 * n + 352 * cells_used
     achieved = alg_bytes / (force_ms / 1e3) / 1e9
     sm_mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     sm_count = device_sm_count(dev)
@@ -326,8 +327,9 @@ def run_ours(args, dist: Dist):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded normal sigma=(1,1,0.2) positions, lognormal masses)",
-        "config": {"workload": WORKLOAD["name"], "n_bodies": n, "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"],
+        "config": {"workload": WORKLOAD["name"] if n == WORKLOAD["n"] else f"bh_plummer_n{n}_theta0.5", "n_bodies": n, "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"],
                    "dt": dt, "G": WORKLOAD["G"], "integrator": "euler", "precision": WORKLOAD["precision"],
+                   "multipole": WORKLOAD["multipole"],
                    "tree": "geometric octree, standard opening criterion, 32-lane warp vote",
                    "l2": "inputs larger than L2 (bodies + tree about 2.3 GB per system)",
                    "parallelism": f"replicas x{dist.world}"},
@@ -363,7 +365,7 @@ def run_reference(args, dist: Dist):
     import nbodysimulation_gb300 as nb
     from nbodysimulation_gb300 import build as nbbuild
     nbbuild.build()
-    n = WORKLOAD["n"]
+    n = args.n
     pos, _, mass = workload_ic(nb, n, seed=0)
     for _ in range(args.warmup):
         cpu_baseline(pos, mass, sample_groups=64)
@@ -390,8 +392,9 @@ def run_reference(args, dist: Dist):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded normal sigma=(1,1,0.2) positions, lognormal masses)",
-        "config": {"workload": WORKLOAD["name"], "n_bodies": n, "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"],
-                   "dt": WORKLOAD["dt"], "precision": WORKLOAD["precision"], "wall_s": wall},
+        "config": {"workload": WORKLOAD["name"] if n == WORKLOAD["n"] else f"bh_plummer_n{n}_theta0.5", "n_bodies": n, "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"],
+                   "dt": WORKLOAD["dt"], "precision": WORKLOAD["precision"], "multipole": WORKLOAD["multipole"],
+                   "wall_s": wall},
         "cpu_baseline": cb,
         "e2e": {"value": value, "unit": "body-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -403,6 +406,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--n", type=int, default=WORKLOAD["n"],
+                    help="bodies per system (default the 4M workload; smaller sizes for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
     ap.add_argument("--skip-fp32", action="store_true", help="omit the plain-FP32 accumulation run")
     args = ap.parse_args()

@@ -93,8 +93,15 @@ enum { NB_TREE_GEOMETRIC = 0, NB_TREE_REFERENCE = 1 };
  * reference's thresholds r^2/theta + eps (calculate_forces.cl:45-61). */
 enum { NB_THETA_STANDARD = 0, NB_THETA_REFERENCE = 1 };
 
-/* Force accumulation precision. */
+/* Force accumulation precision.  NB_PRECISION_COMPENSATED keeps a TwoSum
+ * low word per component; each batch of up to 32 opened children is summed
+ * in FP32 and then added with one TwoSum. */
 enum { NB_PRECISION_FP32 = 0, NB_PRECISION_COMPENSATED = 1 };
+
+/* Cell expansion of the Barnes-Hut force.  NB_MULTIPOLE_MONOPOLE is the
+ * reference's centre-of-mass term; NB_MULTIPOLE_QUADRUPOLE adds each
+ * accepted cell's traceless quadrupole about its centre of mass. */
+enum { NB_MULTIPOLE_MONOPOLE = 0, NB_MULTIPOLE_QUADRUPOLE = 1 };
 
 /* Direct-sum force law.  NB_FORCE_PLUMMER: a = G sum m r (r^2+eps^2)^-3/2.
  * NB_FORCE_REFERENCE_QUIRK: the reference's brute-force arithmetic,
@@ -136,7 +143,8 @@ typedef struct nb_config {
     float mass_lognormal_sigma;        /* NB_MASS_LOGNORMAL, mu = 0, normalised to total 1 */
     uint64_t seed;                     /* initial-condition generator seed */
     int32_t device;                    /* CUDA device ordinal */
-    int32_t reserved[7];
+    int32_t multipole;                 /* NB_MULTIPOLE_MONOPOLE */
+    int32_t reserved[6];
 } nb_config;
 
 typedef struct nb_sim nb_sim;
@@ -192,7 +200,8 @@ enum {
     NB_DEBUG_BODY_COUNT = 4,    /* int32[N+C+1] subtree body counts (cells) */
     NB_DEBUG_SORTED = 5,        /* int32[N] in-order body placement */
     NB_DEBUG_TREE_INFO = 6,     /* int32[4] {N, C (cell capacity), bottom, max_depth} */
-    NB_DEBUG_DQ = 7             /* float[64] opening thresholds of the last force pass */
+    NB_DEBUG_DQ = 7,            /* float[64] opening thresholds of the last force pass */
+    NB_DEBUG_NODE_QUAD = 8      /* float[6*(N+C+1)] cell quadrupoles {xx,yy,zz,xy,xz,yz}, 0 for bodies */
 };
 nb_status nb_get_stage_debug(nb_sim *sim, int32_t which, void *dst, size_t bytes, size_t *written);
 /* Per-stage GPU time in ms, averaged over the steps of the last nb_step

@@ -28,7 +28,8 @@ THETA_STANDARD, THETA_REFERENCE = 0, 1
 PRECISION_FP32, PRECISION_COMPENSATED = 0, 1
 FORCE_PLUMMER, FORCE_REFERENCE_QUIRK = 0, 1
 DEBUG_BBOX, DEBUG_CHILDREN, DEBUG_NODE_POS, DEBUG_NODE_MASS, DEBUG_BODY_COUNT, DEBUG_SORTED, DEBUG_TREE_INFO, \
-    DEBUG_DQ = range(8)
+    DEBUG_DQ, DEBUG_NODE_QUAD = range(9)
+MULTIPOLE_MONOPOLE, MULTIPOLE_QUADRUPOLE = 0, 1
 STAGES = ("bbox", "build", "summarize", "sort", "force", "collision", "direct")
 MAX_DEPTH = 64
 
@@ -66,7 +67,8 @@ class NbConfig(ctypes.Structure):
         ("mass_lognormal_sigma", ctypes.c_float),
         ("seed", ctypes.c_uint64),
         ("device", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("multipole", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
     ]
 
 
@@ -239,7 +241,7 @@ class Simulation:
         need = ctypes.c_size_t(0)
         dummy = np.zeros(1, np.uint8)
         self.L.nb_get_stage_debug(self.h, which, dummy.ctypes.data, 0, ctypes.byref(need))
-        dt = np.float32 if which in (DEBUG_BBOX, DEBUG_NODE_POS, DEBUG_NODE_MASS, DEBUG_DQ) else np.int32
+        dt = np.float32 if which in (DEBUG_BBOX, DEBUG_NODE_POS, DEBUG_NODE_MASS, DEBUG_DQ, DEBUG_NODE_QUAD) else np.int32
         out = np.zeros(need.value // 4, dt)
         self._check(self.L.nb_get_stage_debug(self.h, which, out.ctypes.data, need.value, None),
                     "nb_get_stage_debug")

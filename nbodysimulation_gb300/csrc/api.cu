@@ -44,6 +44,9 @@ struct nb_sim {
     int *parent = nullptr, *child = nullptr, *wchild = nullptr, *count = nullptr, *start = nullptr,
         *arrive = nullptr, *sorted = nullptr;
     float4 *wpm = nullptr, *cell_pm = nullptr;
+    float4 *cell_q = nullptr, *wqa = nullptr;
+    float2 *wqb = nullptr;
+    bool quad = false;
     Ctrl *ctrl = nullptr;
     Ctrl *h_ctrl = nullptr;       // pinned mirror for status read-back
     float *stage3 = nullptr;      // device staging, 3N floats
@@ -100,6 +103,9 @@ static DevSim dev_view(const nb_sim *s) {
     d.arrive = s->arrive;
     d.sorted = s->sorted;
     d.part = s->part;
+    d.cell_q = s->cell_q;
+    d.wqa = s->wqa;
+    d.wqb = s->wqb;
     d.ctrl = s->ctrl;
     return d;
 }
@@ -107,8 +113,10 @@ static DevSim dev_view(const nb_sim *s) {
 static void free_tree(nb_sim *s) {
     cudaFree(s->parent); cudaFree(s->child); cudaFree(s->wchild); cudaFree(s->wpm); cudaFree(s->cell_pm);
     cudaFree(s->count); cudaFree(s->start); cudaFree(s->arrive);
+    cudaFree(s->cell_q); cudaFree(s->wqa); cudaFree(s->wqb);
     s->parent = s->child = s->wchild = s->count = s->start = s->arrive = nullptr;
-    s->wpm = s->cell_pm = nullptr;
+    s->wpm = s->cell_pm = s->cell_q = s->wqa = nullptr;
+    s->wqb = nullptr;
 }
 
 static nb_status alloc_tree(nb_sim *s, int cap) {
@@ -123,6 +131,11 @@ static nb_status alloc_tree(nb_sim *s, int cap) {
     NB_CUDA(s, dalloc(&s->count, cells));
     NB_CUDA(s, dalloc(&s->start, cells));
     NB_CUDA(s, dalloc(&s->arrive, cells));
+    if (s->quad) {
+        NB_CUDA(s, dalloc(&s->cell_q, cells * 2));
+        NB_CUDA(s, dalloc(&s->wqa, cells * 8));
+        NB_CUDA(s, dalloc(&s->wqb, cells * 8));
+    }
     return NB_OK;
 }
 
@@ -220,8 +233,11 @@ nb_status nb_create(const nb_config *cfg, nb_sim **out) {
     cudaMemset(s->vel, 0, sizeof(float4) * n);
     cudaMemset(s->acc, 0, sizeof(float4) * n);
     s->tree = cfg->algo_config == NB_BARNES_HUT;
+    s->quad = cfg->multipole == NB_MULTIPOLE_QUADRUPOLE;
     if (s->tree) {
         int cap = cfg->cell_capacity > 0 ? cfg->cell_capacity : default_capacity(s->n, s->sm_count);
+        // the force walk packs (level << 26) | node into one word
+        if ((long long)s->n + cap + 1 >= (1LL << 26) - 1) return cleanup(NB_ERR_UNSUPPORTED);
         if (alloc_tree(s, cap) != NB_OK) return cleanup(NB_ERR_OUT_OF_MEMORY);
         if (dalloc(&s->sorted, n) != cudaSuccess) return cleanup(NB_ERR_OUT_OF_MEMORY);
     }
@@ -371,6 +387,7 @@ static nb_status enqueue_step(nb_sim *s, float dt, int timed) {
     p.kdk_primed = s->kdk_primed ? 1 : 0;
     p.tree_ref = c.tree_semantics == NB_TREE_REFERENCE;
     p.crit_ref = c.theta_semantics == NB_THETA_REFERENCE;
+    p.quadrupole = s->quad ? 1 : 0;
     DevSim d = dev_view(s);
     cudaStream_t st = s->stream;
     auto mark = [&](int k) {
@@ -385,7 +402,7 @@ static nb_status enqueue_step(nb_sim *s, float dt, int timed) {
         mark(1);
         NB_CUDA(s, launch_build(d, p.tree_ref, s->sm_count, st));
         mark(2);
-        NB_CUDA(s, launch_summarize(d, s->sm_count, st));
+        NB_CUDA(s, launch_summarize(d, p.quadrupole, s->sm_count, st));
         mark(3);
         NB_CUDA(s, launch_sort(d, s->sm_count, st));
         mark(4);
@@ -565,6 +582,7 @@ nb_status nb_get_stage_debug(nb_sim *s, int32_t which, void *dst, size_t bytes, 
     case NB_DEBUG_SORTED: need = n * 4; break;
     case NB_DEBUG_TREE_INFO: need = 4 * 4; break;
     case NB_DEBUG_DQ: need = 64 * 4; break;
+    case NB_DEBUG_NODE_QUAD: need = total * 6 * 4; break;
     default: return fail(s, NB_ERR_INVALID_ARGUMENT, "nb_get_stage_debug: unknown item");
     }
     if (written) *written = need;
@@ -621,7 +639,8 @@ nb_status nb_get_stage_debug(nb_sim *s, int32_t which, void *dst, size_t bytes, 
     cudaError_t e = launch_export_tree(d, which == NB_DEBUG_CHILDREN ? (int *)tmp : nullptr,
                                        which == NB_DEBUG_NODE_POS ? (float *)tmp : nullptr,
                                        which == NB_DEBUG_NODE_MASS ? (float *)tmp : nullptr,
-                                       which == NB_DEBUG_BODY_COUNT ? (int *)tmp : nullptr, s->stream);
+                                       which == NB_DEBUG_BODY_COUNT ? (int *)tmp : nullptr,
+                                       which == NB_DEBUG_NODE_QUAD ? (float *)tmp : nullptr, s->stream);
     s->launches += 1;
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e == cudaSuccess) e = cudaMemcpy(dst, tmp, need, cudaMemcpyDeviceToHost);

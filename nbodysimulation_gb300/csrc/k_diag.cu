@@ -9,7 +9,8 @@ namespace nbgb {
 
 // Reference-layout export (src/MyApp.cpp:219-235): children[8*(N+C+1)] with
 // cell rows at their node index, node positions / masses / body counts.
-__global__ void k_export_tree(DevSim s, int *children_full, float *pos_full, float *mass_full, int *count_full) {
+__global__ void k_export_tree(DevSim s, int *children_full, float *pos_full, float *mass_full, int *count_full,
+                              float *quad_full) {
     const int n = s.n, cap = s.cap, total = n + cap + 1;
     const int bottom = s.ctrl->bottom;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
@@ -39,15 +40,23 @@ __global__ void k_export_tree(DevSim s, int *children_full, float *pos_full, flo
         }
         if (mass_full) mass_full[k] = pm.w;
         if (count_full) count_full[k] = cnt;
+        if (quad_full) {
+            float q[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            if (k >= n && k >= bottom && s.cell_q) {
+                const float4 a = s.cell_q[2 * (k - n)], b = s.cell_q[2 * (k - n) + 1];
+                q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y;
+            }
+            for (int j = 0; j < 6; ++j) quad_full[(size_t)k * 6 + j] = q[j];
+        }
     }
 }
 
 cudaError_t launch_export_tree(const DevSim &s, int *children_full, float *pos_full, float *mass_full,
-                               int *count_full, cudaStream_t st) {
+                               int *count_full, float *quad_full, cudaStream_t st) {
     const int total = s.n + s.cap + 1;
     int blocks = (total + 255) / 256;
     if (blocks > 8192) blocks = 8192;
-    k_export_tree<<<blocks, 256, 0, st>>>(s, children_full, pos_full, mass_full, count_full);
+    k_export_tree<<<blocks, 256, 0, st>>>(s, children_full, pos_full, mass_full, count_full, quad_full);
     return cudaGetLastError();
 }
 

@@ -1,16 +1,23 @@
 // k_force.cu -- Barnes-Hut force walk with the fused integrator
 // (calculate_force_local, kernels/calculate_forces.cl:4-185).
 //
-// One warp owns 32 consecutive bodies of the in-order sort, so its bodies
-// are spatial neighbours.  The warp walks the tree with one shared stack of
-// cells to open (shared memory, 512 entries per warp).  Opening a cell reads
-// its compacted child list (32 B) and the packed {x,y,z,m} of its children
-// (one 128 B line) -- all loads issued at once, one memory round trip per
-// opened cell.  A child body is always accumulated; a child cell is
-// accumulated when EVERY lane of the warp accepts it (__all_sync of
-// d^2 >= dq[level], the reference's work_group_all at :121, here over a real
-// 32-lane warp), otherwise it is pushed.  Softened gravity
-// F = m * rsqrt(d^2)^3 (MUFU rsqrt), d^2 = |d|^2 + eps^2 as FMAs.
+// One warp owns 32 consecutive bodies of the in-order sort (spatial
+// neighbours) and takes its next group from a global counter.  The warp keeps
+// one shared stack of cells still to open.  Each round pops up to kBatch
+// cells and opens them together: lane L loads child slot L%8 of popped cell
+// L/8 -- its index, packed {x,y,z,m} and (with quadrupoles) its moments,
+// coalesced 128-byte lines, one memory round trip for up to 32 children --
+// and stages it in shared memory.  The warp then walks the staged children
+// in order: a child body is always accumulated; a child cell is accumulated
+// when EVERY lane accepts it (__all_sync of d^2 >= dq[level], the
+// reference's work_group_all at :121, over a real 32-lane warp), otherwise it
+// is pushed.  Softened gravity F = m rsqrt(d^2)^3 (MUFU rsqrt), d^2 = |d|^2 +
+// eps^2 as FMAs; accepted cells optionally add their traceless quadrupole.
+//
+// Stack bound: with at most kBatch pops per round only while the stack is
+// under half full, at most 8*kBatch entries per tree level are pending in
+// the first half and 7 per level beyond it, so kStack = 1024 holds any tree
+// of fewer than kMaxDepth levels.  Entries pack (level << 26) | node.
 //
 // The integrator writes the next position buffer, so every force of the step
 // sees step-start positions (the reference integrates in place while other
@@ -19,9 +26,12 @@
 
 namespace nbgb {
 
-constexpr int kForceWarps = 8;
+constexpr int kForceWarps = 4;
 constexpr int kForceThreads = kForceWarps * 32;
-constexpr int kStack = 512;  // >= 7 * kMaxDepth + 1 cells pending per warp
+constexpr int kStack = 1024;
+constexpr int kBatch = 4;
+constexpr int kNodeBits = 26;
+constexpr int kNodeMask = (1 << kNodeBits) - 1;
 
 template <int kMethod>
 __device__ __forceinline__ void integrate_body(const DevSim &s, const StepParams &p, int b, const float4 P, float ax,
@@ -63,6 +73,7 @@ __device__ __forceinline__ void integrate_body(const DevSim &s, const StepParams
     s.body_next[b] = x;
 }
 
+// TwoSum (Knuth): hi + t = s + e exactly; e goes to the low word.
 __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float t) {
     const float s = __fadd_rn(hi, t);
     const float bp = __fsub_rn(s, hi);
@@ -71,10 +82,13 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float t) {
     lo = __fadd_rn(lo, e);
 }
 
-template <int kMethod, bool kComp, bool kEpsZero>
-__global__ void __launch_bounds__(kForceThreads, 2) k_force(DevSim s, StepParams p) {
+template <int kMethod, bool kComp, bool kEpsZero, bool kQuad>
+__global__ void __launch_bounds__(kForceThreads) k_force(DevSim s, StepParams p) {
     __shared__ float s_dq[kMaxDepth];
-    __shared__ int2 s_stack[kForceWarps][kStack];
+    __shared__ int s_stack[kForceWarps][kStack];
+    __shared__ float4 s_pm[kForceWarps][32];
+    __shared__ float4 s_meta[kForceWarps][32];  // {q_xz, q_yz, threshold, packed child}
+    __shared__ float4 s_qa[kForceWarps][kQuad ? 32 : 1];
     __shared__ int s_skip;
     Ctrl *ctrl = s.ctrl;
     const int n = s.n, root = n + s.cap;
@@ -96,59 +110,107 @@ __global__ void __launch_bounds__(kForceThreads, 2) k_force(DevSim s, StepParams
         return;
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int2 *stack = s_stack[w];
+    int *stack = s_stack[w];
+    float4 *spm = s_pm[w];
+    float4 *smeta = s_meta[w];
+    float4 *sqa = s_qa[w];
     const float eps2 = __fmul_rn(p.eps, p.eps);
     const int ngroups = (n + 31) >> 5;
-    const int4 *wchild4 = reinterpret_cast<const int4 *>(s.wchild);
-    for (int g = blockIdx.x * kForceWarps + w; g < ngroups; g += gridDim.x * kForceWarps) {
+    const int cidx = lane >> 3, slot = lane & 7;
+    while (true) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(&ctrl->work, 1);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= ngroups) break;
         const int sidx = g * 32 + lane;
         const bool valid = sidx < n;
         const int b = s.sorted[valid ? sidx : g * 32];
         const float4 P = s.body_cur[b];
         float ax = 0.0f, ay = 0.0f, az = 0.0f, lx = 0.0f, ly = 0.0f, lz = 0.0f;
-        int sp = 1;
         unsigned n_acc = 0, n_open = 0;
-        if (lane == 0) stack[0] = make_int2(root, 0);
+        int sp = 1;
+        if (lane == 0) stack[0] = root;  // level 0
         __syncwarp();
         while (sp > 0) {
-            --sp;
-            const int2 e = stack[sp];
+            const int np = sp > kStack / 2 ? 1 : min(sp, kBatch);
+            sp -= np;
+            n_open += np;
+            // stage: lane L <- child slot L%8 of popped cell L/8
+            float4 pm = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qa = pm, meta = make_float4(0.0f, 0.0f, 0.0f,
+                                                                                        __int_as_float(-1));
+            if (cidx < np) {
+                const int e = stack[sp + cidx];
+                const int node = e & kNodeMask, lv = (int)((unsigned)e >> kNodeBits);
+                const int c = node - n;
+                const int ch = __ldg(&s.wchild[c * 8 + slot]);
+                if (ch >= 0) {
+                    pm = __ldg(&s.wpm[c * 8 + slot]);
+                    float2 qb = make_float2(0.0f, 0.0f);
+                    if constexpr (kQuad) {
+                        if (ch >= n) {
+                            qa = __ldg(&s.wqa[c * 8 + slot]);
+                            qb = __ldg(&s.wqb[c * 8 + slot]);
+                        }
+                    }
+                    meta = make_float4(qb.x, qb.y, s_dq[lv], __int_as_float(((lv + 1) << kNodeBits) | ch));
+                }
+            }
+            __syncwarp();  // every stack entry popped above is read before pushes reuse the slots
+            spm[lane] = pm;
+            smeta[lane] = meta;
+            if constexpr (kQuad) sqa[lane] = qa;
             __syncwarp();
-            const int c = e.x - n;
-            const float thr = s_dq[e.y];
-            ++n_open;
-            const int4 i0 = __ldg(&wchild4[c * 2]);
-            const int4 i1 = __ldg(&wchild4[c * 2 + 1]);
-            float4 q[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) q[j] = __ldg(&s.wpm[c * 8 + j]);
-            const int chs[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int ch = chs[j];
-                if (ch < 0) break;
-                const float dx = q[j].x - P.x, dy = q[j].y - P.y, dz = q[j].z - P.z;
+            float bx = 0.0f, by = 0.0f, bz = 0.0f;  // batch partial sums (compensated mode)
+            const int nk = np * 8;
+            for (int k = 0; k < nk; ++k) {
+                const float4 mt = smeta[k];
+                const int pk = __float_as_int(mt.w);
+                if (pk == -1) continue;
+                const int ch = pk & kNodeMask;
+                const float4 q = spm[k];
+                const float dx = q.x - P.x, dy = q.y - P.y, dz = q.z - P.z;
                 const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-                if (ch < n || __all_sync(0xffffffffu, !valid || d2 >= thr)) {
+                if (ch < n || __all_sync(0xffffffffu, !valid || d2 >= mt.z)) {
                     ++n_acc;
                     const float r = rsqrtf(d2);
-                    float F = (q[j].w * r) * (r * r);
+                    const float r2 = r * r;
+                    float F = (q.w * r) * r2;
                     if constexpr (kEpsZero) F = d2 > 0.0f ? F : 0.0f;
-                    if constexpr (kComp) {
-                        two_sum_add(ax, lx, dx * F);
-                        two_sum_add(ay, ly, dy * F);
-                        two_sum_add(az, lz, dz * F);
-                    } else {
-                        ax = fmaf(dx, F, ax);
-                        ay = fmaf(dy, F, ay);
-                        az = fmaf(dz, F, az);
+                    float ux = dx * F, uy = dy * F, uz = dz * F;
+                    if constexpr (kQuad) {
+                        if (ch >= n) {  // 2.5 (d.Q.d) d / r^7 - Q d / r^5
+                            const float4 Q = sqa[k];  // xx yy zz xy; mt.x = xz, mt.y = yz
+                            const float qx = fmaf(mt.x, dz, fmaf(Q.w, dy, Q.x * dx));
+                            const float qy = fmaf(mt.y, dz, fmaf(Q.y, dy, Q.w * dx));
+                            const float qz = fmaf(Q.z, dz, fmaf(mt.y, dy, mt.x * dx));
+                            const float sq = fmaf(dz, qz, fmaf(dy, qy, dx * qx));
+                            const float r5 = (r * r2) * r2;
+                            const float c1 = (2.5f * sq) * (r5 * r2);
+                            ux += fmaf(dx, c1, -qx * r5);
+                            uy += fmaf(dy, c1, -qy * r5);
+                            uz += fmaf(dz, c1, -qz * r5);
+                        }
                     }
-                } else if (sp < kStack && e.y + 1 < kMaxDepth) {
-                    if (lane == 0) stack[sp] = make_int2(ch, e.y + 1);
+                    if constexpr (kComp) {
+                        bx += ux;
+                        by += uy;
+                        bz += uz;
+                    } else {
+                        ax += ux;
+                        ay += uy;
+                        az += uz;
+                    }
+                } else if (sp < kStack) {
+                    if (lane == 0) stack[sp] = pk;
                     ++sp;
-                } else if (lane == 0) {  // cannot happen below kMaxDepth levels; never overrun
-                    set_status(ctrl, kStDepth, e.y + 1);
+                } else if (lane == 0) {  // outside the stack bound: never overrun shared memory
+                    set_status(ctrl, kStDepth, kStack);
                 }
+            }
+            if constexpr (kComp) {  // one TwoSum per batch into the running sum
+                two_sum_add(ax, lx, bx);
+                two_sum_add(ay, ly, by);
+                two_sum_add(az, lz, bz);
             }
             __syncwarp();
         }
@@ -169,27 +231,39 @@ __global__ void __launch_bounds__(kForceThreads, 2) k_force(DevSim s, StepParams
     }
 }
 
-template <int kMethod, bool kComp>
+template <int kMethod, bool kComp, bool kQuad>
 static cudaError_t launch_force_t(const DevSim &s, const StepParams &p, int sm_count, cudaStream_t st) {
     const bool ez = !(p.eps > 0.0f);
-    const void *fn = ez ? (const void *)k_force<kMethod, kComp, true> : (const void *)k_force<kMethod, kComp, false>;
+    const void *fn = ez ? (const void *)k_force<kMethod, kComp, true, kQuad>
+                        : (const void *)k_force<kMethod, kComp, false, kQuad>;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kForceThreads, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     int blocks = per_sm * sm_count;
     const int need = ((s.n + 31) / 32 + kForceWarps - 1) / kForceWarps;
     if (blocks > need) blocks = need > 0 ? need : 1;
-    if (ez) k_force<kMethod, kComp, true><<<blocks, kForceThreads, 0, st>>>(s, p);
-    else k_force<kMethod, kComp, false><<<blocks, kForceThreads, 0, st>>>(s, p);
+    if (ez) k_force<kMethod, kComp, true, kQuad><<<blocks, kForceThreads, 0, st>>>(s, p);
+    else k_force<kMethod, kComp, false, kQuad><<<blocks, kForceThreads, 0, st>>>(s, p);
     return cudaGetLastError();
+}
+
+template <int kMethod>
+static cudaError_t launch_force_m(const DevSim &s, const StepParams &p, int compensated, int sm_count,
+                                  cudaStream_t st) {
+    if (p.quadrupole) {
+        return compensated ? launch_force_t<kMethod, true, true>(s, p, sm_count, st)
+                           : launch_force_t<kMethod, false, true>(s, p, sm_count, st);
+    }
+    return compensated ? launch_force_t<kMethod, true, false>(s, p, sm_count, st)
+                       : launch_force_t<kMethod, false, false>(s, p, sm_count, st);
 }
 
 cudaError_t launch_force(const DevSim &s, const StepParams &p, int compensated, int sm_count, cudaStream_t st) {
     switch (p.method) {
-    case 1: return compensated ? launch_force_t<1, true>(s, p, sm_count, st) : launch_force_t<1, false>(s, p, sm_count, st);
-    case 2: return compensated ? launch_force_t<2, true>(s, p, sm_count, st) : launch_force_t<2, false>(s, p, sm_count, st);
-    case 3: return compensated ? launch_force_t<3, true>(s, p, sm_count, st) : launch_force_t<3, false>(s, p, sm_count, st);
-    default: return compensated ? launch_force_t<0, true>(s, p, sm_count, st) : launch_force_t<0, false>(s, p, sm_count, st);
+    case 1: return launch_force_m<1>(s, p, compensated, sm_count, st);
+    case 2: return launch_force_m<2>(s, p, compensated, sm_count, st);
+    case 3: return launch_force_m<3>(s, p, compensated, sm_count, st);
+    default: return launch_force_m<0>(s, p, compensated, sm_count, st);
     }
 }
 

@@ -270,6 +270,7 @@ __device__ __forceinline__ void load_children(const int *child, int c, int chs[8
 // the update that completes a cell; child-cell data written in this kernel is
 // read through L2 (__ldcg).
 // ---------------------------------------------------------------------------
+template <bool kQuad>
 __global__ void __launch_bounds__(256) k_summarize(DevSim s) {
     if (read_status(s.ctrl)) return;
     const int n = s.n, root = n + s.cap;
@@ -327,8 +328,40 @@ __global__ void __launch_bounds__(256) k_summarize(DevSim s) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) prow[q] = wp[q];
             const float inv = __frcp_rn(M);
+            const float X = __fmul_rn(cx, inv), Y = __fmul_rn(cy, inv), Z = __fmul_rn(cz, inv);
             s.count[c] = cnt;
-            s.cell_pm[c] = make_float4(__fmul_rn(cx, inv), __fmul_rn(cy, inv), __fmul_rn(cz, inv), M);
+            s.cell_pm[c] = make_float4(X, Y, Z, M);
+            if constexpr (kQuad) {
+                // traceless quadrupole about the centre of mass, children in
+                // slot order: Q += Q_child + m (3 d d^T - |d|^2 I), d = x_child - X
+                float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f, q3 = 0.0f, q4 = 0.0f, q5 = 0.0f;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int ch = wc[j];
+                    if (ch < 0) break;
+                    const float4 pm = wp[j];
+                    float4 oa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    float4 ob = oa;
+                    if (ch >= n) {
+                        oa = __ldcg(&s.cell_q[2 * (ch - n)]);
+                        ob = __ldcg(&s.cell_q[2 * (ch - n) + 1]);
+                    }
+                    s.wqa[c * 8 + j] = oa;
+                    s.wqb[c * 8 + j] = make_float2(ob.x, ob.y);
+                    const float m = pm.w;
+                    const float dx = __fsub_rn(pm.x, X), dy = __fsub_rn(pm.y, Y), dz = __fsub_rn(pm.z, Z);
+                    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                    const float tx = __fmul_rn(3.0f, dx), ty = __fmul_rn(3.0f, dy);
+                    q0 = __fadd_rn(q0, __fmaf_rn(m, __fmaf_rn(tx, dx, -r2), oa.x));
+                    q1 = __fadd_rn(q1, __fmaf_rn(m, __fmaf_rn(ty, dy, -r2), oa.y));
+                    q2 = __fadd_rn(q2, __fmaf_rn(m, __fmaf_rn(__fmul_rn(3.0f, dz), dz, -r2), oa.z));
+                    q3 = __fadd_rn(q3, __fmaf_rn(m, __fmul_rn(tx, dy), oa.w));
+                    q4 = __fadd_rn(q4, __fmaf_rn(m, __fmul_rn(tx, dz), ob.x));
+                    q5 = __fadd_rn(q5, __fmaf_rn(m, __fmul_rn(ty, dz), ob.y));
+                }
+                s.cell_q[2 * c] = make_float4(q0, q1, q2, q3);
+                s.cell_q[2 * c + 1] = make_float4(q4, q5, 0.0f, 0.0f);
+            }
             if (node == root) break;
             const int p = s.parent[c];
             load_children(s.child, p - n, chs, nch, nbody, n);
@@ -425,11 +458,12 @@ cudaError_t launch_build(const DevSim &s, int tree_ref, int sm_count, cudaStream
     return cudaGetLastError();
 }
 
-cudaError_t launch_summarize(const DevSim &s, int sm_count, cudaStream_t st) {
+cudaError_t launch_summarize(const DevSim &s, int quadrupole, int sm_count, cudaStream_t st) {
     int blocks = sm_count * 8;
     const int need = (s.cap + 1 + 255) / 256;
     if (blocks > need) blocks = need > 0 ? need : 1;
-    k_summarize<<<blocks, 256, 0, st>>>(s);
+    if (quadrupole) k_summarize<true><<<blocks, 256, 0, st>>>(s);
+    else k_summarize<false><<<blocks, 256, 0, st>>>(s);
     return cudaGetLastError();
 }
 

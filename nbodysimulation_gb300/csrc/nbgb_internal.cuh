@@ -62,7 +62,10 @@ struct DevSim {
     int *start;
     int *arrive;
     int *sorted;
-    float4 *part;  // N partial accelerations of a split direct sum
+    float4 *part;    // N partial accelerations of a split direct sum
+    float4 *cell_q;  // 2 per cell: {xx, yy, zz, xy}, {xz, yz, 0, 0} about the centre of mass
+    float4 *wqa;     // (C+1)*8: quadrupole {xx, yy, zz, xy} of each packed child (0 for bodies)
+    float2 *wqb;     // (C+1)*8: {xz, yz} of each packed child
     Ctrl *ctrl;
 };
 
@@ -75,6 +78,7 @@ struct StepParams {
     int kdk_primed;
     int tree_ref;    // reference tree semantics
     int crit_ref;    // reference opening thresholds
+    int quadrupole;  // accepted cells add their quadrupole term
 };
 
 __device__ __forceinline__ unsigned f2key(float f) {
@@ -128,7 +132,7 @@ struct LaunchShape {
 cudaError_t launch_reset(const DevSim &s, cudaStream_t st);
 cudaError_t launch_bbox(const DevSim &s, int sm_count, cudaStream_t st);
 cudaError_t launch_build(const DevSim &s, int tree_ref, int sm_count, cudaStream_t st);
-cudaError_t launch_summarize(const DevSim &s, int sm_count, cudaStream_t st);
+cudaError_t launch_summarize(const DevSim &s, int quadrupole, int sm_count, cudaStream_t st);
 cudaError_t launch_sort(const DevSim &s, int sm_count, cudaStream_t st);
 cudaError_t launch_force(const DevSim &s, const StepParams &p, int compensated, int sm_count, cudaStream_t st);
 cudaError_t launch_direct(const DevSim &s, const StepParams &p, int tiled, int quirk, int sm_count,
@@ -140,7 +144,7 @@ cudaError_t launch_pack(const float *pos3, const float *mass, const float *vel3,
 cudaError_t launch_unpack(const float4 *body, const float4 *vel, const float4 *acc, float *pos3, float *vel3,
                           float *acc3, int n, cudaStream_t st);
 cudaError_t launch_export_tree(const DevSim &s, int *children_full, float *pos_full, float *mass_full,
-                               int *count_full, cudaStream_t st);
+                               int *count_full, float *quad_full, cudaStream_t st);
 cudaError_t launch_force_probe(const float4 *body, int n, const int *sample, int ns, double eps, double G,
                                double *out3, cudaStream_t st);
 cudaError_t launch_diagnostics(const float4 *body, const float4 *vel, int n, int with_potential, double eps,

@@ -346,6 +346,35 @@ int orc_saturate(int compaction_bug, int n, int nodes, int bottom, float *node_p
     return ORC_OK;
 }
 
+/* Traceless quadrupole of every cell about its centre of mass (an addition:
+ * the reference is monopole only).  Bottom-up in slot order:
+ * Q += Q_child + m_child (3 d d^T - |d|^2 I), d = x_child - x_cell; a body has
+ * Q = 0.  quad[6*node] = {xx, yy, zz, xy, xz, yz}. */
+void orc_quadrupoles(int n, int nodes, int bottom, const float *node_pos, const float *node_mass,
+                     const int *children, float *quad) {
+    const int root = n + nodes;
+    for (long i = 0; i < (long)(n + nodes + 1) * 6; ++i) quad[i] = 0.0f;
+    for (int c = bottom; c <= root; ++c) {
+        const int *row = children + (long)c * 8;
+        const float X = node_pos[c * 3 + 0], Y = node_pos[c * 3 + 1], Z = node_pos[c * 3 + 2];
+        float q[6] = {0, 0, 0, 0, 0, 0};
+        for (int s = 0; s < 8; ++s) {
+            const int ch = row[s];
+            if (ch < 0) continue;
+            const float m = node_mass[ch];
+            const float dx = node_pos[ch * 3 + 0] - X, dy = node_pos[ch * 3 + 1] - Y, dz = node_pos[ch * 3 + 2] - Z;
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float t[6] = {fmaf(3.0f * dx, dx, -r2), fmaf(3.0f * dy, dy, -r2), fmaf(3.0f * dz, dz, -r2),
+                                3.0f * dx * dy, 3.0f * dx * dz, 3.0f * dy * dz};
+            for (int k = 0; k < 6; ++k) {
+                const float own = ch >= n ? quad[(long)ch * 6 + k] : 0.0f;
+                q[k] = q[k] + fmaf(m, t[k], own);
+            }
+        }
+        for (int k = 0; k < 6; ++k) quad[(long)c * 6 + k] = q[k];
+    }
+}
+
 /* ------------------------------------------------------------------ */
 /* Sort (the reference's sort.cl is empty)                              */
 /* ------------------------------------------------------------------ */
@@ -422,10 +451,13 @@ void orc_bh_thresholds(int criterion, const float box6[6], float theta, float ep
  * skip_self: a body does not interact with itself (the reference includes
  *   the self pair, which adds exactly zero when eps > 0).
  * compensated: per-component TwoSum accumulation (acc = hi + lo).
+ * quad: optional cell quadrupoles (6 per node, orc_quadrupoles); accepted
+ *   cells then add the softened quadrupole term.
+ * stats: optional {body interactions, cell interactions} (per lane).
  * acc3 receives G*acc.  Returns 0, or ORC_ERR_DEPTH on stack overflow. */
 int orc_bh_force(const float *node_pos, const float *node_mass, const int *children, int n, int nodes,
                  const float *dq, float eps, float G, int arith, int vote_width, const int *order, int norder,
-                 int skip_self, int compensated, float *acc3) {
+                 int skip_self, int compensated, const float *quad, long long *stats, float *acc3) {
     const int root = n + nodes;
     if (vote_width < 1 || vote_width > 64) return ORC_ERR_ARG;
     if (!order || norder <= 0 || norder > n) norder = n;
@@ -453,6 +485,7 @@ int orc_bh_force(const float *node_pos, const float *node_mass, const int *child
         st_node[0] = root;
         st_pos[0] = 0;
         int local_err = 0;
+        long long nb_body = 0, nb_cell = 0;
         while (depth >= 0 && !local_err) {
             int top;
             while ((top = st_pos[depth]) < 8) {
@@ -499,6 +532,33 @@ int orc_bh_force(const float *node_pos, const float *node_mass, const int *child
                                 s = ay[l] + ty; bp = s - ay[l]; e = (ay[l] - (s - bp)) + (ty - bp); ay[l] = s; ly[l] += e;
                                 s = az[l] + tz; bp = s - az[l]; e = (az[l] - (s - bp)) + (tz - bp); az[l] = s; lz[l] += e;
                             }
+                            if (quad && child >= n) {
+                                /* softened quadrupole of the cell about its centre of mass:
+                                 * a += 2.5 (d.Q.d) d / r^7 - Q d / r^5, d = x_cell - x_body */
+                                const float *Q = quad + (long)child * 6; /* xx yy zz xy xz yz */
+                                const float dx = dxv[l], dy = dyv[l], dz = dzv[l];
+                                const float qx = fmaf(Q[4], dz, fmaf(Q[3], dy, Q[0] * dx));
+                                const float qy = fmaf(Q[5], dz, fmaf(Q[1], dy, Q[3] * dx));
+                                const float qz = fmaf(Q[2], dz, fmaf(Q[5], dy, Q[4] * dx));
+                                const float sq = fmaf(dz, qz, fmaf(dy, qy, dx * qx));
+                                const float r2i = r * r;
+                                const float r5 = (r * r2i) * r2i;
+                                const float c1 = (2.5f * sq) * (r5 * r2i);
+                                const float ux = fmaf(dx, c1, -qx * r5), uy = fmaf(dy, c1, -qy * r5),
+                                            uz = fmaf(dz, c1, -qz * r5);
+                                if (!compensated) {
+                                    ax[l] += ux; ay[l] += uy; az[l] += uz;
+                                } else {
+                                    float s, bp, e;
+                                    s = ax[l] + ux; bp = s - ax[l]; e = (ax[l] - (s - bp)) + (ux - bp); ax[l] = s; lx[l] += e;
+                                    s = ay[l] + uy; bp = s - ay[l]; e = (ay[l] - (s - bp)) + (uy - bp); ay[l] = s; ly[l] += e;
+                                    s = az[l] + uz; bp = s - az[l]; e = (az[l] - (s - bp)) + (uz - bp); az[l] = s; lz[l] += e;
+                                }
+                            }
+                            if (stats) {
+                                if (child < n) ++nb_body;
+                                else ++nb_cell;
+                            }
                         }
                     } else {
                         ++depth;
@@ -515,6 +575,12 @@ int orc_bh_force(const float *node_pos, const float *node_mass, const int *child
         if (local_err) {
 #pragma omp atomic write
             err = ORC_ERR_DEPTH;
+        }
+        if (stats) {
+#pragma omp atomic
+            stats[0] += nb_body;
+#pragma omp atomic
+            stats[1] += nb_cell;
         }
         for (int l = 0; l < lanes; ++l) {
             float x = ax[l], y = ay[l], z = az[l];

@@ -47,7 +47,8 @@ def lib():
             "orc_saturate": ([i, i, i, i, P, P, P, P], i),
             "orc_sort": ([P, i, i, P], i),
             "orc_bh_thresholds": ([i, P, f, f, i, P], None),
-            "orc_bh_force": ([P, P, P, i, i, P, f, f, i, i, P, i, i, i, P], i),
+            "orc_bh_force": ([P, P, P, i, i, P, f, f, i, i, P, i, i, i, P, P, P], i),
+            "orc_quadrupoles": ([i, i, i, P, P, P, P], None),
             "orc_direct_fp32": ([P, P, i, f, f, i, i, P], None),
             "orc_direct_fp64": ([P, P, i, d, d, P, i, P], None),
             "orc_direct_quirk_global": ([P, P, i, f, P], None),
@@ -168,15 +169,25 @@ def thresholds(criterion, box6, theta, eps, max_depth):
     return dq
 
 
+def quadrupoles(t: Tree):
+    q = np.zeros((t.n + t.nodes + 1) * 6, np.float32)
+    lib().orc_quadrupoles(t.n, t.nodes, t.bottom, _p(t.pos), _p(t.mass), _p(i32(t.children)), _p(q))
+    return q
+
+
 def bh_force(t: Tree, dq, eps, G, arith=ARITH_FMA, vote_width=32, order=None, skip_self=True,
-             compensated=False):
+             compensated=False, quad=None, stats=None):
     """Forces for the bodies of `order` (all bodies when None), walked in
-    groups of `vote_width` consecutive entries."""
+    groups of `vote_width` consecutive entries.  `quad` (from quadrupoles())
+    adds the cells' quadrupole terms; `stats` (int64[2]) receives the body and
+    cell interaction counts."""
     acc = np.zeros(t.n * 3, np.float32)
     order = i32(order) if order is not None else None
     norder = 0 if order is None else len(order)
+    q = f32(quad) if quad is not None else None
     rc = lib().orc_bh_force(_p(t.pos), _p(t.mass), _p(t.children), t.n, t.nodes, _p(f32(dq)), eps, G, arith,
-                            vote_width, _p(order), norder, 1 if skip_self else 0, 1 if compensated else 0, _p(acc))
+                            vote_width, _p(order), norder, 1 if skip_self else 0, 1 if compensated else 0, _p(q),
+                            _p(stats), _p(acc))
     return acc.reshape(-1, 3), rc
 
 
@@ -243,7 +254,7 @@ def copy_vertices(pos3):
 
 
 def bh_step_forces(pos3, mass, theta, eps, G, sem=SEM_GEOMETRIC, criterion=CRIT_STANDARD, arith=ARITH_FMA,
-                   vote_width=32, order="sorted", compensated=False, nodes=None, box=None):
+                   vote_width=32, order="sorted", compensated=False, nodes=None, box=None, quadrupole=False):
     """bbox -> build -> summarise -> sort -> force, as the GPU library runs it.
     Returns (acc[N,3], tree, sorted)."""
     pos3 = f32(pos3).reshape(-1, 3)
@@ -257,7 +268,8 @@ def bh_step_forces(pos3, mass, theta, eps, G, sem=SEM_GEOMETRIC, criterion=CRIT_
     srt, k = sort_bodies(t.children, t.n, t.root)
     dq = thresholds(criterion, box, theta, eps, t.max_depth)
     o = srt if order == "sorted" else (None if order is None else order)
-    acc, rc = bh_force(t, dq, eps, G, arith=arith, vote_width=vote_width, order=o, compensated=compensated)
+    q = quadrupoles(t) if quadrupole else None
+    acc, rc = bh_force(t, dq, eps, G, arith=arith, vote_width=vote_width, order=o, compensated=compensated, quad=q)
     if rc:
         raise RuntimeError(f"oracle force failed: {rc}")
     return acc, t, srt
