@@ -41,7 +41,8 @@ WORKLOAD = dict(name="bh_plummer_n4m_theta0.5", n=4194304, sigma=(1.0, 1.0, 0.2)
                 eps=0.005, dt=1e-3, G=1.0, precision="compensated", multipole="quadrupole")
 PROBE_SAMPLES = 8192
 FP32_LANES_PER_SM = 128
-FLOPS_PER_INTERACTION = 12  # FP32-pipe instructions per interaction (3 sub, 3 fma, 3 mul, 3 fma)
+FLOPS_PER_INTERACTION = 12  # FP32 ops per monopole interaction (3 sub, 3 fma, 3 mul, 3 fma)
+FLOPS_PER_QUADRUPOLE = 19   # extra FP32 ops per cell quadrupole term (Q.d 9, d.Q.d 3, r^5 r^7 2, 2.5*sq 1, 4 fma)
 
 
 # ---------------------------------------------------------------------------
@@ -245,7 +246,7 @@ def run_ours(args, dist: Dist):
     dist.barrier()
     launches = sim.kernel_launches() - launches0
     stage = sim.timings()
-    inter, opened = sim.work_counters()
+    inter, opened, cell_inter = sim.work_counters()
     info = sim.stage_debug(nb.DEBUG_TREE_INFO)
     cells_used = int(info[0] + info[1] - info[2] + 1)
     ms_max = dist.max(ms)
@@ -307,7 +308,8 @@ def run_ours(args, dist: Dist):
     sm_mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     sm_count = device_sm_count(dev)
     inter_per_step = inter / args.steps
-    fp32_peak = FP32_LANES_PER_SM * sm_count * sm_mhz * 1e6 / FLOPS_PER_INTERACTION
+    flops_per_step = (FLOPS_PER_INTERACTION * inter + FLOPS_PER_QUADRUPOLE * cell_inter) / args.steps
+    fp32_peak_ops = FP32_LANES_PER_SM * sm_count * sm_mhz * 1e6  # one FP32 op per lane per clock
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "force_traffic.json")
     if os.path.exists(tfile):
@@ -344,12 +346,15 @@ def run_ours(args, dist: Dist):
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "algorithmic_bytes": alg_bytes, "peak_kind": f"{peak_kind} hbm copy",
                      "note": "the force walk is latency / FP32-bound; see compute"},
-        "compute": {"bound": "fp32", "interactions_per_step": inter_per_step,
+        "compute": {"bound": "fp32", "kernel": "k_force", "interactions_per_step": inter_per_step,
+                    "cell_interactions_per_step": cell_inter / args.steps,
                     "interactions_per_s": inter_per_step / (force_ms / 1e3),
-                    "peak_interactions_per_s": fp32_peak,
-                    "frac": (inter_per_step / (force_ms / 1e3)) / fp32_peak,
+                    "achieved_gops": flops_per_step / (force_ms / 1e3) / 1e9,
+                    "peak_gops": fp32_peak_ops / 1e9,
+                    "frac": flops_per_step / (force_ms / 1e3) / fp32_peak_ops,
                     "cells_opened_per_step": opened / args.steps,
-                    "peak_kind": "derived: 128 FP32 lanes x SMs x median sampled SM clock / 12"},
+                    "ops_model": "12 FP32 ops per interaction + 19 per cell quadrupole term",
+                    "peak_kind": "derived: 128 FP32 lanes x SMs x median sampled SM clock"},
         "tree": {"cells_used": cells_used, "max_depth": int(info[3])},
         "clocks": clk,
     }

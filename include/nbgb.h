@@ -216,8 +216,9 @@ int64_t nb_kernel_launches(const nb_sim *sim);
  * device time of the nsteps steps. */
 nb_status nb_time_steps(nb_sim *sim, float dt, int32_t nsteps, float *total_ms);
 /* Work of the last nb_step call: out[0] body-node interactions of the force
- * passes (per body, per accepted node), out[1] cells opened by the warps. */
-nb_status nb_get_work_counters(nb_sim *sim, uint64_t out[2]);
+ * passes (per body, per accepted node), out[1] cells opened by the warps,
+ * out[2] the part of out[0] with cells (the rest are body-body pairs). */
+nb_status nb_get_work_counters(nb_sim *sim, uint64_t out[3]);
 
 /* ---- device-resident access (interop, benchmarking) ---- */
 typedef struct nb_device_view {

@@ -262,9 +262,10 @@ class Simulation:
         return ms.value
 
     def work_counters(self):
-        out = np.zeros(2, np.uint64)
+        """(interactions, cells opened, cell interactions) of the last nb_step call."""
+        out = np.zeros(3, np.uint64)
         self._check(self.L.nb_get_work_counters(self.h, out.ctypes.data), "nb_get_work_counters")
-        return int(out[0]), int(out[1])
+        return int(out[0]), int(out[1]), int(out[2])
 
     def kernel_launches(self):
         return int(self.L.nb_kernel_launches(self.h))

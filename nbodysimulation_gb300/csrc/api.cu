@@ -525,10 +525,11 @@ nb_status nb_time_steps(nb_sim *s, float dt, int32_t nsteps, float *total_ms) {
     return r;
 }
 
-nb_status nb_get_work_counters(nb_sim *s, uint64_t out[2]) {
+nb_status nb_get_work_counters(nb_sim *s, uint64_t out[3]) {
     if (!s || !out) return NB_ERR_INVALID_ARGUMENT;
     out[0] = s->h_ctrl->interactions;
     out[1] = s->h_ctrl->opened;
+    out[2] = s->h_ctrl->cell_interactions;
     return NB_OK;
 }
 

@@ -14,10 +14,12 @@
 // is pushed.  Softened gravity F = m rsqrt(d^2)^3 (MUFU rsqrt), d^2 = |d|^2 +
 // eps^2 as FMAs; accepted cells optionally add their traceless quadrupole.
 //
-// Stack bound: with at most kBatch pops per round only while the stack is
-// under half full, at most 8*kBatch entries per tree level are pending in
-// the first half and 7 per level beyond it, so kStack = 1024 holds any tree
-// of fewer than kMaxDepth levels.  Entries pack (level << 26) | node.
+// Stack bound: kBatch cells are popped only while the stack holds at most
+// kBatchBelow entries, so a batch leaves at most kBatchBelow - 1 + 8*kBatch
+// entries; beyond that the walk pops one cell at a time (depth first), which
+// adds at most 7 pending siblings per tree level: at most 127 + 32 + 7*63 + 1
+// = 601 <= kStack entries for any tree of fewer than kMaxDepth levels.
+// Entries pack (level << 26) | node.
 //
 // The integrator writes the next position buffer, so every force of the step
 // sees step-start positions (the reference integrates in place while other
@@ -28,8 +30,9 @@ namespace nbgb {
 
 constexpr int kForceWarps = 4;
 constexpr int kForceThreads = kForceWarps * 32;
-constexpr int kStack = 1024;
+constexpr int kStack = 640;
 constexpr int kBatch = 4;
+constexpr int kBatchBelow = 128;  // batch pops only while the stack holds at most this many
 constexpr int kNodeBits = 26;
 constexpr int kNodeMask = (1 << kNodeBits) - 1;
 
@@ -86,9 +89,10 @@ template <int kMethod, bool kComp, bool kEpsZero, bool kQuad>
 __global__ void __launch_bounds__(kForceThreads) k_force(DevSim s, StepParams p) {
     __shared__ float s_dq[kMaxDepth];
     __shared__ int s_stack[kForceWarps][kStack];
-    __shared__ float4 s_pm[kForceWarps][32];
-    __shared__ float4 s_meta[kForceWarps][32];  // {q_xz, q_yz, threshold, packed child}
-    __shared__ float4 s_qa[kForceWarps][kQuad ? 32 : 1];
+    __shared__ float4 s_bpm[kForceWarps][32];                 // staged child bodies {x,y,z,m}
+    __shared__ float4 s_cpm[kForceWarps][32];                 // staged child cells {x,y,z,m}
+    __shared__ float4 s_cmeta[kForceWarps][32];               // {q_xz, q_yz, threshold, packed child}
+    __shared__ float4 s_cqa[kForceWarps][kQuad ? 32 : 1];     // {q_xx, q_yy, q_zz, q_xy}
     __shared__ int s_skip;
     Ctrl *ctrl = s.ctrl;
     const int n = s.n, root = n + s.cap;
@@ -111,12 +115,14 @@ __global__ void __launch_bounds__(kForceThreads) k_force(DevSim s, StepParams p)
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int *stack = s_stack[w];
-    float4 *spm = s_pm[w];
-    float4 *smeta = s_meta[w];
-    float4 *sqa = s_qa[w];
+    float4 *bpm = s_bpm[w];
+    float4 *cpm = s_cpm[w];
+    float4 *cmeta = s_cmeta[w];
+    float4 *cqa = s_cqa[w];
     const float eps2 = __fmul_rn(p.eps, p.eps);
     const int ngroups = (n + 31) >> 5;
     const int cidx = lane >> 3, slot = lane & 7;
+    const unsigned below = (1u << lane) - 1u;
     while (true) {
         int g = 0;
         if (lane == 0) g = atomicAdd(&ctrl->work, 1);
@@ -124,84 +130,99 @@ __global__ void __launch_bounds__(kForceThreads) k_force(DevSim s, StepParams p)
         if (g >= ngroups) break;
         const int sidx = g * 32 + lane;
         const bool valid = sidx < n;
+        // a lane past the end takes lane 0's body: its votes copy lane 0's,
+        // so the warp vote needs no validity test; its result is discarded
         const int b = s.sorted[valid ? sidx : g * 32];
         const float4 P = s.body_cur[b];
         float ax = 0.0f, ay = 0.0f, az = 0.0f, lx = 0.0f, ly = 0.0f, lz = 0.0f;
-        unsigned n_acc = 0, n_open = 0;
+        unsigned n_body = 0, n_cell = 0, n_open = 0;
         int sp = 1;
         if (lane == 0) stack[0] = root;  // level 0
         __syncwarp();
         while (sp > 0) {
-            const int np = sp > kStack / 2 ? 1 : min(sp, kBatch);
+            const int np = sp > kBatchBelow ? 1 : min(sp, kBatch);
             sp -= np;
             n_open += np;
-            // stage: lane L <- child slot L%8 of popped cell L/8
-            float4 pm = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qa = pm, meta = make_float4(0.0f, 0.0f, 0.0f,
-                                                                                        __int_as_float(-1));
+            // lane L loads child slot L%8 of popped cell L/8
+            int ch = -1;
+            float4 pm = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qa = pm;
+            float2 qb = make_float2(0.0f, 0.0f);
+            float thr = 0.0f;
+            int lv = 0;
             if (cidx < np) {
                 const int e = stack[sp + cidx];
-                const int node = e & kNodeMask, lv = (int)((unsigned)e >> kNodeBits);
-                const int c = node - n;
-                const int ch = __ldg(&s.wchild[c * 8 + slot]);
+                const int c = (e & kNodeMask) - n;
+                lv = (int)((unsigned)e >> kNodeBits);
+                ch = __ldg(&s.wchild[c * 8 + slot]);
                 if (ch >= 0) {
                     pm = __ldg(&s.wpm[c * 8 + slot]);
-                    float2 qb = make_float2(0.0f, 0.0f);
+                    thr = s_dq[lv];
                     if constexpr (kQuad) {
                         if (ch >= n) {
                             qa = __ldg(&s.wqa[c * 8 + slot]);
                             qb = __ldg(&s.wqb[c * 8 + slot]);
                         }
                     }
-                    meta = make_float4(qb.x, qb.y, s_dq[lv], __int_as_float(((lv + 1) << kNodeBits) | ch));
                 }
             }
-            __syncwarp();  // every stack entry popped above is read before pushes reuse the slots
-            spm[lane] = pm;
-            smeta[lane] = meta;
-            if constexpr (kQuad) sqa[lane] = qa;
+            // compact: bodies and cells in two dense lists, slot order kept
+            const bool isb = ch >= 0 && ch < n, isc = ch >= n;
+            const unsigned mb = __ballot_sync(0xffffffffu, isb), mc = __ballot_sync(0xffffffffu, isc);
+            __syncwarp();  // the popped stack entries are read before pushes reuse them
+            if (isb) bpm[__popc(mb & below)] = pm;
+            if (isc) {
+                const int k = __popc(mc & below);
+                cpm[k] = pm;
+                cmeta[k] = make_float4(qb.x, qb.y, thr, __int_as_float(((lv + 1) << kNodeBits) | ch));
+                if constexpr (kQuad) cqa[k] = qa;
+            }
             __syncwarp();
-            float bx = 0.0f, by = 0.0f, bz = 0.0f;  // batch partial sums (compensated mode)
-            const int nk = np * 8;
-            for (int k = 0; k < nk; ++k) {
-                const float4 mt = smeta[k];
-                const int pk = __float_as_int(mt.w);
-                if (pk == -1) continue;
-                const int ch = pk & kNodeMask;
-                const float4 q = spm[k];
+            const int nb = __popc(mb), nc = __popc(mc);
+            float bx = 0.0f, by = 0.0f, bz = 0.0f;  // batch sums (compensated mode)
+            float &sx = kComp ? bx : ax, &sy = kComp ? by : ay, &sz = kComp ? bz : az;
+            // child bodies: always accumulated
+            n_body += nb;
+#pragma unroll 2
+            for (int k = 0; k < nb; ++k) {
+                const float4 q = bpm[k];
                 const float dx = q.x - P.x, dy = q.y - P.y, dz = q.z - P.z;
                 const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-                if (ch < n || __all_sync(0xffffffffu, !valid || d2 >= mt.z)) {
-                    ++n_acc;
+                const float r = rsqrtf(d2);
+                float F = q.w * (r * (r * r));
+                if constexpr (kEpsZero) F = d2 > 0.0f ? F : 0.0f;
+                sx = fmaf(dx, F, sx);
+                sy = fmaf(dy, F, sy);
+                sz = fmaf(dz, F, sz);
+            }
+            // child cells: accumulated when every lane accepts, else pushed
+            for (int k = 0; k < nc; ++k) {
+                const float4 q = cpm[k];
+                const float4 mt = cmeta[k];
+                const float dx = q.x - P.x, dy = q.y - P.y, dz = q.z - P.z;
+                const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+                if (__all_sync(0xffffffffu, d2 >= mt.z)) {
+                    ++n_cell;
                     const float r = rsqrtf(d2);
                     const float r2 = r * r;
-                    float F = (q.w * r) * r2;
-                    if constexpr (kEpsZero) F = d2 > 0.0f ? F : 0.0f;
-                    float ux = dx * F, uy = dy * F, uz = dz * F;
-                    if constexpr (kQuad) {
-                        if (ch >= n) {  // 2.5 (d.Q.d) d / r^7 - Q d / r^5
-                            const float4 Q = sqa[k];  // xx yy zz xy; mt.x = xz, mt.y = yz
-                            const float qx = fmaf(mt.x, dz, fmaf(Q.w, dy, Q.x * dx));
-                            const float qy = fmaf(mt.y, dz, fmaf(Q.y, dy, Q.w * dx));
-                            const float qz = fmaf(Q.z, dz, fmaf(mt.y, dy, mt.x * dx));
-                            const float sq = fmaf(dz, qz, fmaf(dy, qy, dx * qx));
-                            const float r5 = (r * r2) * r2;
-                            const float c1 = (2.5f * sq) * (r5 * r2);
-                            ux += fmaf(dx, c1, -qx * r5);
-                            uy += fmaf(dy, c1, -qy * r5);
-                            uz += fmaf(dz, c1, -qz * r5);
-                        }
+                    const float r3 = r * r2;
+                    float F = q.w * r3;
+                    if constexpr (kQuad) {  // + 2.5 (d.Q.d) d / r^7 - Q d / r^5
+                        const float4 Q = cqa[k];  // xx yy zz xy; mt.x = xz, mt.y = yz
+                        const float qx = fmaf(mt.x, dz, fmaf(Q.w, dy, Q.x * dx));
+                        const float qy = fmaf(mt.y, dz, fmaf(Q.y, dy, Q.w * dx));
+                        const float qz = fmaf(Q.z, dz, fmaf(mt.y, dy, mt.x * dx));
+                        const float sq = fmaf(dz, qz, fmaf(dy, qy, dx * qx));
+                        const float r5 = r3 * r2;
+                        F = fmaf(2.5f * sq, r5 * r2, F);
+                        sx = fmaf(-qx, r5, sx);
+                        sy = fmaf(-qy, r5, sy);
+                        sz = fmaf(-qz, r5, sz);
                     }
-                    if constexpr (kComp) {
-                        bx += ux;
-                        by += uy;
-                        bz += uz;
-                    } else {
-                        ax += ux;
-                        ay += uy;
-                        az += uz;
-                    }
+                    sx = fmaf(dx, F, sx);
+                    sy = fmaf(dy, F, sy);
+                    sz = fmaf(dz, F, sz);
                 } else if (sp < kStack) {
-                    if (lane == 0) stack[sp] = pk;
+                    if (lane == 0) stack[sp] = __float_as_int(mt.w);
                     ++sp;
                 } else if (lane == 0) {  // outside the stack bound: never overrun shared memory
                     set_status(ctrl, kStDepth, kStack);
@@ -216,7 +237,8 @@ __global__ void __launch_bounds__(kForceThreads) k_force(DevSim s, StepParams p)
         }
         if (lane == 0) {
             const unsigned lanes = (unsigned)min(32, n - g * 32);
-            atomicAdd(&ctrl->interactions, (unsigned long long)n_acc * lanes);
+            atomicAdd(&ctrl->interactions, (unsigned long long)(n_body + n_cell) * lanes);
+            atomicAdd(&ctrl->cell_interactions, (unsigned long long)n_cell * lanes);
             atomicAdd(&ctrl->opened, (unsigned long long)n_open);
         }
         if constexpr (kComp) {

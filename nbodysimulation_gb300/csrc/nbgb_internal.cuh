@@ -44,6 +44,7 @@ struct Ctrl {
     int status_info;
     unsigned long long interactions;  // body-node interactions of the force passes
     unsigned long long opened;        // cells opened by the force passes
+    unsigned long long cell_interactions;  // the part of `interactions` with cells
 };
 
 struct DevSim {
