@@ -154,3 +154,47 @@ def test_invalid_arguments_without_device(nbgb_lib):
     assert L.nb_create(ct.byref(c), ct.byref(h)) == nbgb_lib.ERR_INVALID_ARGUMENT
     assert L.nb_step(None, 0.001, 1) == nbgb_lib.ERR_INVALID_ARGUMENT
     assert L.nb_destroy(None) == nbgb_lib.ERR_INVALID_ARGUMENT
+
+
+CPP_PROGRAM = r'''
+#include <cstdio>
+#include "nbgb.hpp"
+int main() {
+    nb::SimulationConfig c;
+    if (c.GetNumberOfBodies() != 20000 || c.GetBarnesHutConfig().GetTheta() != 1.5f) return 2;
+    c.SetNumberOfBodies(1024);
+    c.SetAlgorithmConfig(nb::BARNES_HUT);
+    c.GetBarnesHutConfig().SetTheta(0.5f);
+    nb_config cc = c.ToC();
+    if (cc.num_of_bodies != 1024 || cc.algo_config != NB_BARNES_HUT || cc.theta != 0.5f) return 3;
+    nb::NBodyApp app;
+    app.NextConfig() = c;
+    try {
+        app.ResetSimulation();
+        nb::SUpdateInfo u;
+        u.DeltaTimeInSec = 0.016f;
+        app.Update(u);
+        std::vector<float> p, v, m;
+        app.GetState(p, v, m);
+        std::printf("stepped %zu\n", m.size());
+    } catch (const nb::Error &e) {
+        std::printf("error %d\n", (int)e.status);
+    }
+    return 0;
+}
+'''
+
+
+def test_cpp_host_mirror_compiles_and_links(nbgb_lib, tmp_path):
+    """include/nbgb.hpp (the C++ mirror of the reference's host classes) builds
+    against the C ABI and runs: it steps on a GPU, or reports NB_ERR_NO_DEVICE."""
+    src = tmp_path / "app.cpp"
+    src.write_text(CPP_PROGRAM)
+    exe = tmp_path / "app"
+    libdir = os.path.dirname(nbgb_lib.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lnbgb",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert r.stdout.startswith("stepped 1024") or r.stdout.strip() in (f"error {nbgb_lib.ERR_NO_DEVICE}",
+                                                                          f"error {nbgb_lib.ERR_CUDA}")
