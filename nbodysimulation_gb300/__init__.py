@@ -110,7 +110,9 @@ SIGNATURES = {
     "nb_last_error_message": ([_P], ctypes.c_char_p),
     "nb_host_alloc": ([_SZ], _P),
     "nb_host_free": ([_P], None),
+    "nb_direct_accel_noalloc": ([_P, _I, _F, _F, _P, _P], _I),
 }
+NOALLOC_MAX_BODIES = 65536
 
 _lib = None
 

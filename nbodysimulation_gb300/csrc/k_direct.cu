@@ -439,3 +439,144 @@ cudaError_t launch_unpack(const float4 *body, const float4 *vel, const float4 *a
 }
 
 }  // namespace nbgb
+
+namespace nbgb {
+
+// ===========================================================================
+// Allocation-free all-pairs accelerations (nb_direct_accel_noalloc).
+//
+// For callers that must not allocate device memory: a host engine that owns
+// the whole device-memory budget and hands the library only its own buffers,
+// or a frame loop where a cudaMalloc (which can synchronise the device and
+// take an allocator lock) is not allowed.  The caller passes the bodies and
+// the output; the one piece of scratch the split all-pairs sum needs -- the
+// partial accelerations of the j slices -- lives in a file-scope device
+// array of fixed size, together with a status word for the bounded waits.
+// Every GPU that loads this library holds that array (1 MiB + 80 B) until
+// the process exits.  All calls share it: calls that overlap on the GPU race.
+// ===========================================================================
+constexpr int kNoAllocMaxBodies = 65536;  // = NB_NOALLOC_MAX_BODIES
+static __device__ __align__(256) float4 g_noalloc_part[kNoAllocMaxBodies];
+static __device__ __align__(256) Ctrl g_noalloc_ctrl;
+
+// The tiled all-pairs kernel above with the j range split over gridDim.y and
+// every slice adding its partial sums into `part`; no integrator.
+template <bool kEpsZero>
+__global__ void __launch_bounds__(kDirectThreads) k_noalloc_partial(const float4 *__restrict__ body, int n,
+                                                                     float eps2, float4 *part, Ctrl *ctrl) {
+    __shared__ __align__(128) float4 tile[2][kTile];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int ntiles = (n + kTile - 1) / kTile;
+    const int per_split = (ntiles + gridDim.y - 1) / gridDim.y;
+    const int t0 = blockIdx.y * per_split;
+    const int t1 = min(ntiles, t0 + per_split);
+    const int i = blockIdx.x * kDirectThreads + threadIdx.x;
+    const float4 me = i < n ? body[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float ax = 0.0f, ay = 0.0f, az = 0.0f;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](int t, int stage) {
+        const int cnt = min(kTile, n - t * kTile);
+        const uint32_t bytes = (uint32_t)cnt * 16u;
+        mbar_expect_tx(&bar[stage], bytes);
+        bulk_g2s(&tile[stage][0], body + (size_t)t * kTile, bytes, &bar[stage]);
+    };
+    if (threadIdx.x == 0 && t0 < t1) issue(t0, 0);
+    bool ok = true;
+    for (int t = t0; t < t1; ++t) {
+        const int it = t - t0;
+        const int stage = it & 1;
+        if (threadIdx.x == 0 && t + 1 < t1) issue(t + 1, stage ^ 1);
+        if (!mbar_wait_bounded(&bar[stage], (uint32_t)((it >> 1) & 1), ctrl)) ok = false;
+        const int cnt = min(kTile, n - t * kTile);
+        for (int j = 0; j < cnt; ++j) pair<false, kEpsZero>(me, tile[stage][j], eps2, ax, ay, az);
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0 && t + 1 < t1)
+                mbar_wait_bounded(&bar[stage ^ 1], (uint32_t)(((it + 1) >> 1) & 1), ctrl);
+            ok = false;
+            break;
+        }
+    }
+    if (!ok || i >= n) return;
+    atomicAdd(&part[i].x, ax);
+    atomicAdd(&part[i].y, ay);
+    atomicAdd(&part[i].z, az);
+}
+
+__global__ void k_noalloc_finish(const float4 *__restrict__ part, int n, float G, float4 *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = part[i];
+    out[i] = make_float4(a.x * G, a.y * G, a.z * G, 0.0f);
+}
+
+}  // namespace nbgb
+
+#include <mutex>
+
+#include "../../include/nbgb.h"
+
+namespace {
+// Device addresses of the two arrays, looked up once per device with that
+// device current.  In host code the array names are host-side stand-ins, not
+// device addresses, so only these looked-up pointers are passed to kernels.
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_part_ptr[kMaxDevices] = {};
+void *g_noalloc_ctrl_ptr[kMaxDevices] = {};
+
+bool noalloc_setup(int dev, float4 **part, nbgb::Ctrl **ctrl) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_part_ptr[dev]) {
+        void *p = nullptr, *c = nullptr;
+        if (cudaGetSymbolAddress(&p, nbgb::g_noalloc_part) != cudaSuccess) return false;
+        if (cudaGetSymbolAddress(&c, nbgb::g_noalloc_ctrl) != cudaSuccess) return false;
+        g_noalloc_part_ptr[dev] = p;
+        g_noalloc_ctrl_ptr[dev] = c;
+    }
+    *part = static_cast<float4 *>(g_noalloc_part_ptr[dev]);
+    *ctrl = static_cast<nbgb::Ctrl *>(g_noalloc_ctrl_ptr[dev]);
+    return true;
+}
+}  // namespace
+
+extern "C" nb_status nb_direct_accel_noalloc(const float *d_body4, int32_t n, float eps, float G, float *d_acc4,
+                                            void *stream) {
+    using namespace nbgb;
+    if (!d_body4 || !d_acc4 || n < 1 || !(eps >= 0.0f)) return NB_ERR_INVALID_ARGUMENT;
+    if (n > kNoAllocMaxBodies) return NB_ERR_INVALID_ARGUMENT;  // beyond the fixed scratch
+    if (((uintptr_t)d_body4 & 15u) || ((uintptr_t)d_acc4 & 15u)) return NB_ERR_INVALID_ARGUMENT;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return NB_ERR_NO_DEVICE;
+    float4 *part = nullptr;
+    Ctrl *ctrl = nullptr;
+    if (!noalloc_setup(dev, &part, &ctrl)) return NB_ERR_CUDA;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the scratch keeps the previous call's contents: clear what must start at 0
+    if (cudaMemsetAsync(part, 0, sizeof(float4) * (size_t)n, st) != cudaSuccess) return NB_ERR_CUDA;
+    if (cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), st) != cudaSuccess) return NB_ERR_CUDA;
+    int sm_count = 0;
+    cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+    const int bx = (n + kDirectThreads - 1) / kDirectThreads;
+    const int ntiles = (n + kTile - 1) / kTile;
+    int split = (2 * sm_count + bx - 1) / bx;
+    if (split > ntiles) split = ntiles;
+    if (split < 1) split = 1;
+    const float eps2 = eps * eps;
+    const float4 *body = reinterpret_cast<const float4 *>(d_body4);
+    if (eps > 0.0f) k_noalloc_partial<false><<<dim3(bx, split), kDirectThreads, 0, st>>>(body, n, eps2, part, ctrl);
+    else k_noalloc_partial<true><<<dim3(bx, split), kDirectThreads, 0, st>>>(body, n, eps2, part, ctrl);
+    k_noalloc_finish<<<bx, kDirectThreads, 0, st>>>(part, n, G, reinterpret_cast<float4 *>(d_acc4));
+    if (cudaGetLastError() != cudaSuccess) return NB_ERR_CUDA;
+    // wait, then read the status of the bounded waits (no allocation: a
+    // stack variable receives it)
+    int status = 0;
+    if (cudaMemcpyAsync(&status, &ctrl->status, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return NB_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return NB_ERR_CUDA;
+    return status ? (nb_status)status : NB_OK;
+}
