@@ -276,6 +276,41 @@ void nb_host_free(void *p);
 nb_status nb_direct_accel_noalloc(const float *d_body4, int32_t n, float eps, float G, float *d_acc4,
                                   void *stream);
 
+/* ---- batched systems ----
+ * Many independent simulations of uneven N advanced together, each with its
+ * own nb_config (the reference runs one CMyApp per simulation,
+ * src/MyApp.cpp:110-656).  Every stage of a step is one kernel launch over
+ * all systems, and one step is replayed as a CUDA graph.  Systems with
+ * algo_config NB_BARNES_HUT take the tree path, the others the tiled direct
+ * sum.  All systems must share numerical_method, precision, multipole and
+ * device; epsilon (direct_epsilon for direct systems) must be > 0; the
+ * reference quirk force law and collisions are not batched.  Each system's
+ * step is the same computation as nb_step on a standalone handle: the tree
+ * path is bit-identical, the direct sum differs only in summation order. */
+typedef struct nb_batch nb_batch;
+nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out);
+nb_status nb_batch_destroy(nb_batch *b);
+/* State of system k (host arrays, reference layout); vel3 may be NULL (zero). */
+nb_status nb_batch_set_state(nb_batch *b, int32_t k, const float *pos3, const float *vel3, const float *mass);
+nb_status nb_batch_get_state(nb_batch *b, int32_t k, float *pos3, float *vel3, float *acc3, float *mass);
+/* nsteps steps of all systems with time step dt; returns the first failing
+ * system's status (the others advanced normally; a failed system keeps the
+ * state it had at the start of the failing step). */
+nb_status nb_batch_step(nb_batch *b, float dt, int32_t nsteps);
+/* As nb_batch_step, timed with CUDA events around the graph launches. */
+nb_status nb_batch_time_steps(nb_batch *b, float dt, int32_t nsteps, float *total_ms);
+/* Status of system k after the last nb_batch_step. */
+nb_status nb_batch_system_status(nb_batch *b, int32_t k);
+/* Chooses the direct-sum kernel shape by timing the candidates on this
+ * batch (state unchanged); the choice is cached in the JSON file cache_path
+ * (may be NULL) under a key of the SM count and the batch's size profile. */
+nb_status nb_batch_autotune(nb_batch *b, const char *cache_path, int32_t *chosen);
+/* out: systems, bodies, tree systems, direct systems, launches per step,
+ * direct variant, kernels launched so far, body-node interactions of the
+ * last step (tree systems). */
+nb_status nb_batch_info(nb_batch *b, int64_t out[8]);
+const char *nb_batch_last_error_message(const nb_batch *b);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

@@ -111,6 +111,16 @@ SIGNATURES = {
     "nb_host_alloc": ([_SZ], _P),
     "nb_host_free": ([_P], None),
     "nb_direct_accel_noalloc": ([_P, _I, _F, _F, _P, _P], _I),
+    "nb_batch_create": ([_P, _I, ctypes.POINTER(_P)], _I),
+    "nb_batch_destroy": ([_P], _I),
+    "nb_batch_set_state": ([_P, _I, _P, _P, _P], _I),
+    "nb_batch_get_state": ([_P, _I, _P, _P, _P, _P], _I),
+    "nb_batch_step": ([_P, _F, _I], _I),
+    "nb_batch_time_steps": ([_P, _F, _I, ctypes.POINTER(_F)], _I),
+    "nb_batch_system_status": ([_P, _I], _I),
+    "nb_batch_autotune": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
+    "nb_batch_info": ([_P, _P], _I),
+    "nb_batch_last_error_message": ([_P], ctypes.c_char_p),
 }
 NOALLOC_MAX_BODIES = 65536
 
@@ -290,3 +300,88 @@ class Simulation:
         self._check(self.L.nb_diagnostics(self.h, 1 if with_potential else 0, out.ctypes.data), "nb_diagnostics")
         keys = ("kinetic", "px", "py", "pz", "lx", "ly", "lz", "mass", "potential")
         return dict(zip(keys, out.tolist()))
+
+
+class Batch:
+    """Many independent systems advanced together (nb_batch_*): one launch per
+    stage over all systems, one CUDA graph per step."""
+
+    def __init__(self, cfgs):
+        self.L = load()
+        self.cfgs = list(cfgs)
+        arr = (NbConfig * len(self.cfgs))(*self.cfgs)
+        h = ctypes.c_void_p()
+        st = self.L.nb_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(self.cfgs), ctypes.byref(h))
+        if st:
+            raise NbError(st, f"nb_batch_create: {self.L.nb_status_string(st).decode()}")
+        self.h = h
+        self.ns = [c.num_of_bodies for c in self.cfgs]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.nb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __len__(self):
+        return len(self.ns)
+
+    def _check(self, st, what):
+        if st:
+            msg = self.L.nb_batch_last_error_message(self.h).decode()
+            raise NbError(st, f"{what}: {msg or self.L.nb_status_string(st).decode()}")
+
+    def set_state(self, k, pos, mass, vel=None):
+        pos = _f32(pos, (-1,))
+        mass = _f32(mass, (-1,))
+        v = None if vel is None else _f32(vel, (-1,))
+        self._check(self.L.nb_batch_set_state(self.h, k, pos.ctypes.data, None if v is None else v.ctypes.data,
+                                              mass.ctypes.data), "nb_batch_set_state")
+
+    def get_state(self, k):
+        n = self.ns[k]
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        acc = np.zeros((n, 3), np.float32)
+        mass = np.zeros(n, np.float32)
+        self._check(self.L.nb_batch_get_state(self.h, k, pos.ctypes.data, vel.ctypes.data, acc.ctypes.data,
+                                              mass.ctypes.data), "nb_batch_get_state")
+        return pos, vel, acc, mass
+
+    def step(self, dt, nsteps=1, check=True):
+        st = self.L.nb_batch_step(self.h, dt, nsteps)
+        if check:
+            self._check(st, "nb_batch_step")
+        return st
+
+    def time_steps(self, dt, nsteps):
+        ms = ctypes.c_float(0.0)
+        self._check(self.L.nb_batch_time_steps(self.h, dt, nsteps, ctypes.byref(ms)), "nb_batch_time_steps")
+        return ms.value
+
+    def system_status(self, k):
+        return int(self.L.nb_batch_system_status(self.h, k))
+
+    def autotune(self, cache_path=None):
+        chosen = ctypes.c_int32(-1)
+        path = None if cache_path is None else os.fsencode(cache_path)
+        self._check(self.L.nb_batch_autotune(self.h, path, ctypes.byref(chosen)), "nb_batch_autotune")
+        return chosen.value
+
+    def info(self):
+        out = np.zeros(8, np.int64)
+        self._check(self.L.nb_batch_info(self.h, out.ctypes.data), "nb_batch_info")
+        keys = ("systems", "bodies", "tree_systems", "direct_systems", "launches_per_step", "direct_variant",
+                "launches", "interactions")
+        return dict(zip(keys, (int(x) for x in out)))

@@ -1,0 +1,427 @@
+// k_batch.cu -- one launch per stage for many independent systems of uneven
+// N.  Every kernel walks the batch's table of systems (SysDesc): the work
+// of all systems is laid end to end in one index space per stage (bodies in
+// chunks, cell slots, warp groups, direct-sum target blocks) and a thread
+// finds its system with a binary search in the stage's prefix table.
+// Barnes-Hut systems run the same per-item code as the single-system
+// kernels (bh_device.cuh, force_device.cuh); small systems take the
+// TMA-tiled direct sum.  A step is: reset, bbox, build, summarize, sort,
+// force, direct, flip -- captured once into a CUDA graph by the host.
+#include "bh_device.cuh"
+#include "force_device.cuh"
+#include "tma.cuh"
+
+namespace nbgb {
+
+constexpr int kChunk = kBatchChunk;
+
+// ---------------------------------------------------------------------------
+// reset (init, kernels/init.cl:26-33) for every Barnes-Hut system
+// ---------------------------------------------------------------------------
+__global__ void k_batch_reset(BatchTables t) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= t.nsys) return;
+    const SysDesc &d = t.sys[k];
+    if (!d.active || d.kind != kSysBH) return;
+    const DevSim &s = d.v;
+    Ctrl *c = s.ctrl;
+    c->bbox_key[0] = c->bbox_key[1] = c->bbox_key[2] = 0xFFFFFFFFu;
+    c->bbox_key[3] = c->bbox_key[4] = c->bbox_key[5] = 0u;
+    int4 *row = reinterpret_cast<int4 *>(&s.child[s.cap * 8]);
+    row[0] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+    row[1] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+    c->bottom = s.n + s.cap;
+    c->max_depth = 0;
+    c->work = 0;
+    s.arrive[s.cap] = 0;
+    s.start[s.cap] = 0;
+    s.count[s.cap] = 0;
+    s.parent[s.cap] = -1;
+}
+
+// ---------------------------------------------------------------------------
+// bbox: one block per chunk of one system; order-preserving integer keys,
+// one atomic per component per block (as k_bbox)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_batch_bbox(BatchTables t) {
+    const int k = find_system(t.chunk_prefix, t.nsys, blockIdx.x);
+    const SysDesc &d = t.sys[k];
+    const DevSim s = system_view(d);
+    const int i0 = (blockIdx.x - d.chunk_begin) * kChunk;
+    const int i1 = min(s.n, i0 + kChunk);
+    unsigned mn0 = 0xFFFFFFFFu, mn1 = 0xFFFFFFFFu, mn2 = 0xFFFFFFFFu, mx0 = 0u, mx1 = 0u, mx2 = 0u;
+    int bad = -1;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const float4 p = __ldg(&s.body_cur[i]);
+        if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) bad = i;
+        const unsigned kx = f2key(p.x), ky = f2key(p.y), kz = f2key(p.z);
+        mn0 = min(mn0, kx); mx0 = max(mx0, kx);
+        mn1 = min(mn1, ky); mx1 = max(mx1, ky);
+        mn2 = min(mn2, kz); mx2 = max(mx2, kz);
+    }
+    mn0 = __reduce_min_sync(0xffffffffu, mn0);
+    mn1 = __reduce_min_sync(0xffffffffu, mn1);
+    mn2 = __reduce_min_sync(0xffffffffu, mn2);
+    mx0 = __reduce_max_sync(0xffffffffu, mx0);
+    mx1 = __reduce_max_sync(0xffffffffu, mx1);
+    mx2 = __reduce_max_sync(0xffffffffu, mx2);
+    __shared__ unsigned red[8][6];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        red[w][0] = mn0; red[w][1] = mn1; red[w][2] = mn2;
+        red[w][3] = mx0; red[w][4] = mx1; red[w][5] = mx2;
+    }
+    if (bad >= 0) set_status(s.ctrl, kStNonFinite, bad);
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int c = threadIdx.x;
+        unsigned v = red[0][c];
+        for (int j = 1; j < 8; ++j) v = c < 3 ? min(v, red[j][c]) : max(v, red[j][c]);
+        if (c < 3) atomicMin(&s.ctrl->bbox_key[c], v);
+        else atomicMax(&s.ctrl->bbox_key[c], v);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// build: one block per chunk of one system (insert_body), one max-depth
+// atomic per block.  Lock holders are always running threads, so no
+// co-residency is needed.
+// ---------------------------------------------------------------------------
+template <class Geo, bool kRef>
+__device__ __forceinline__ int build_chunk(const DevSim &s, int i0, int i1) {
+    float box[6];
+    load_box(s.ctrl, box);
+    const Geo root_g = Geo::root(box);
+    int local_max = 0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int depth = insert_body<Geo, kRef>(s, root_g, i);
+        if (depth < 0) return -1;
+        local_max = max(local_max, depth);
+    }
+    return local_max;
+}
+
+__global__ void __launch_bounds__(256) k_batch_build(BatchTables t) {
+    const int k = find_system(t.chunk_prefix, t.nsys, blockIdx.x);
+    const SysDesc &d = t.sys[k];
+    const DevSim s = system_view(d);
+    if (read_status(s.ctrl)) return;
+    const int i0 = (blockIdx.x - d.chunk_begin) * kChunk;
+    const int i1 = min(s.n, i0 + kChunk);
+    const int depth = d.p.tree_ref ? build_chunk<RefBox, true>(s, i0, i1) : build_chunk<GeoCube, false>(s, i0, i1);
+    if (depth < 0) return;
+    const unsigned am = __activemask();
+    const int wmax = __reduce_max_sync(am, depth);
+    if ((threadIdx.x & 31) == __ffs(am) - 1) atomicMax(&s.ctrl->max_depth, wmax);
+}
+
+// ---------------------------------------------------------------------------
+// summarize: one cell slot per thread over all systems' slot ranges
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < t.cells; x += stride) {
+        const int k = find_system(t.cell_prefix, t.nsys, x);
+        const SysDesc &d = t.sys[k];
+        const DevSim s = system_view(d);
+        if (read_status(s.ctrl)) continue;
+        const int node = s.n + (x - d.cell_begin);
+        if (node < s.ctrl->bottom) continue;
+        if (d.p.quadrupole) summarize_from<true>(s, node);
+        else summarize_from<false>(s, node);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// sort: inside every system the slots are visited in descending node order
+// (a parent before its children); the grid is no larger than what is
+// co-resident, so every bounded wait in sort_cell is for a cell another
+// running thread handles in an earlier or the same round.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_batch_sort(BatchTables t) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < t.cells; x += stride) {
+        const int k = find_system(t.cell_prefix, t.nsys, x);
+        const SysDesc &d = t.sys[k];
+        const DevSim s = system_view(d);
+        if (read_status(s.ctrl)) continue;
+        const int node = s.n + s.cap - (x - d.cell_begin);
+        if (node < s.ctrl->bottom) continue;
+        sort_cell(s, node);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// force: warps take groups from one batch-wide counter; a warp recomputes its
+// thresholds whenever its next group belongs to another system.  A system
+// whose step failed keeps its step-start state.
+// ---------------------------------------------------------------------------
+template <int kMethod, bool kComp, bool kQuad>
+__global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
+    __shared__ float s_dq[kForceWarps][kMaxDepth];
+    __shared__ int s_stack[kForceWarps][kStack];
+    __shared__ float4 s_bpm[kForceWarps][32];
+    __shared__ float4 s_cpm[kForceWarps][32];
+    __shared__ float4 s_cmeta[kForceWarps][32];
+    __shared__ float4 s_cqa[kForceWarps][kQuad ? 32 : 1];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const WarpStage ws{s_stack[w], s_bpm[w], s_cpm[w], s_cmeta[w], s_cqa[w]};
+    float *dq = s_dq[w];
+    int cur = -1;
+    bool skip = false;
+    while (true) {
+        int gg = 0;
+        if (lane == 0) gg = atomicAdd(t.work, 1);
+        gg = __shfl_sync(0xffffffffu, gg, 0);
+        if (gg >= t.groups) break;
+        const int k = find_system(t.group_prefix, t.nsys, gg);
+        const SysDesc &d = t.sys[k];
+        const DevSim s = system_view(d);
+        StepParams p = d.p;
+        p.kdk_primed = s.ctrl->kdk_primed;
+        if (k != cur) {
+            cur = k;
+            int sk = 0;
+            if (lane == 0) {
+                sk = read_status(s.ctrl);
+                if (!sk && s.ctrl->max_depth >= kMaxDepth) {
+                    set_status(s.ctrl, kStDepth, s.ctrl->max_depth);
+                    sk = 1;
+                }
+            }
+            skip = __shfl_sync(0xffffffffu, sk, 0) != 0;
+            __syncwarp();  // the previous system's thresholds are no longer read
+            if (lane == 0) {
+                float box[6];
+                load_box(s.ctrl, box);
+                make_thresholds(box, p.theta, p.eps, p.crit_ref, dq);
+            }
+            __syncwarp();
+        }
+        const int g = gg - d.group_begin;
+        if (skip) {  // keep the step-start state
+            const int i = g * 32 + lane;
+            if (i < s.n) s.body_next[i] = s.body_cur[i];
+            continue;
+        }
+        force_group<kMethod, kComp, false, kQuad>(s, p, dq, g, lane, ws);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// direct: one block per kThreads*kI targets of one system; j-tiles of kTileB
+// bodies staged by TMA bulk copies (double-buffered mbarriers); Plummer
+// softening; fused integrator.  kI, kThreads and kTileB come from the
+// autotuner.
+// ---------------------------------------------------------------------------
+template <int kI, int kThreads, int kTileB>
+__global__ void __launch_bounds__(kThreads) k_batch_direct(BatchTables t) {
+    __shared__ __align__(128) float4 tile[2][kTileB];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int k = find_system(t.dblock_prefix, t.nsys, blockIdx.x);
+    const SysDesc &d = t.sys[k];
+    const DevSim s = system_view(d);
+    StepParams p = d.p;
+    p.kdk_primed = s.ctrl->kdk_primed;
+    const int n = s.n;
+    const int base = (blockIdx.x - d.dblock_begin) * (kThreads * kI);
+    const float eps2 = p.eps * p.eps;
+    int idx[kI];
+    float4 me[kI];
+    float ax[kI], ay[kI], az[kI];
+#pragma unroll
+    for (int r = 0; r < kI; ++r) {
+        idx[r] = base + r * kThreads + threadIdx.x;
+        me[r] = idx[r] < n ? s.body_cur[idx[r]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        ax[r] = ay[r] = az[r] = 0.0f;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const int ntiles = (n + kTileB - 1) / kTileB;
+    auto issue = [&](int tt, int stage) {
+        const int cnt = min(kTileB, n - tt * kTileB);
+        const uint32_t bytes = (uint32_t)cnt * 16u;
+        mbar_expect_tx(&bar[stage], bytes);
+        bulk_g2s(&tile[stage][0], s.body_cur + (size_t)tt * kTileB, bytes, &bar[stage]);
+    };
+    if (threadIdx.x == 0 && ntiles > 0) issue(0, 0);
+    bool ok = true;
+    for (int tt = 0; tt < ntiles; ++tt) {
+        const int stage = tt & 1;
+        if (threadIdx.x == 0 && tt + 1 < ntiles) issue(tt + 1, stage ^ 1);
+        if (!mbar_wait_bounded(&bar[stage], (uint32_t)((tt >> 1) & 1), s.ctrl)) ok = false;
+        const int cnt = min(kTileB, n - tt * kTileB);
+        const float4 *tl = tile[stage];
+#pragma unroll 4
+        for (int j = 0; j < cnt; ++j) {
+            const float4 q = tl[j];
+#pragma unroll
+            for (int r = 0; r < kI; ++r) {
+                const float dx = q.x - me[r].x, dy = q.y - me[r].y, dz = q.z - me[r].z;
+                const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+                const float rr = rsqrtf(d2);
+                const float F = (q.w * rr) * (rr * rr);
+                ax[r] = fmaf(dx, F, ax[r]);
+                ay[r] = fmaf(dy, F, ay[r]);
+                az[r] = fmaf(dz, F, az[r]);
+            }
+        }
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0 && tt + 1 < ntiles)
+                mbar_wait_bounded(&bar[stage ^ 1], (uint32_t)(((tt + 1) >> 1) & 1), s.ctrl);
+            ok = false;
+            break;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kI; ++r) {
+        if (idx[r] >= n) continue;
+        if (!ok) {
+            s.body_next[idx[r]] = me[r];
+            continue;
+        }
+        const float gx = ax[r] * p.G, gy = ay[r] * p.G, gz = az[r] * p.G;
+        switch (p.method) {
+        case 1: integrate_body<1>(s, p, idx[r], me[r], gx, gy, gz); break;
+        case 2: integrate_body<2>(s, p, idx[r], me[r], gx, gy, gz); break;
+        case 3: integrate_body<3>(s, p, idx[r], me[r], gx, gy, gz); break;
+        default: integrate_body<0>(s, p, idx[r], me[r], gx, gy, gz); break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// flip: the next buffer becomes current; KDK systems are primed
+// ---------------------------------------------------------------------------
+__global__ void k_batch_flip(BatchTables t) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= t.nsys) return;
+    const SysDesc &d = t.sys[k];
+    if (!d.active) return;
+    d.v.ctrl->parity ^= 1;
+    if (d.p.method == 3) d.v.ctrl->kdk_primed = 1;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static int resident(const void *fn, int threads, int sm_count) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * sm_count;
+}
+
+// Direct-sum variants the autotuner chooses from: {bodies per thread,
+// threads per block, j-tile bodies}.
+struct DirectVariant {
+    int ki, threads, tile;
+};
+static const DirectVariant kDirectVariants[] = {{1, 128, 128}, {1, 128, 256}, {1, 256, 256}, {2, 128, 128},
+                                                {2, 128, 256}, {2, 256, 256}, {4, 128, 256}, {4, 256, 256}};
+constexpr int kNumDirectVariants = sizeof(kDirectVariants) / sizeof(kDirectVariants[0]);
+
+int batch_direct_variants() { return kNumDirectVariants; }
+int batch_direct_block_bodies(int variant) {
+    const DirectVariant &v = kDirectVariants[variant];
+    return v.ki * v.threads;
+}
+
+static cudaError_t launch_direct_variant(const BatchTables &t, int variant, cudaStream_t st) {
+    const int b = t.dblocks;
+    switch (variant) {
+    case 0: k_batch_direct<1, 128, 128><<<b, 128, 0, st>>>(t); break;
+    case 1: k_batch_direct<1, 128, 256><<<b, 128, 0, st>>>(t); break;
+    case 2: k_batch_direct<1, 256, 256><<<b, 256, 0, st>>>(t); break;
+    case 3: k_batch_direct<2, 128, 128><<<b, 128, 0, st>>>(t); break;
+    case 4: k_batch_direct<2, 128, 256><<<b, 128, 0, st>>>(t); break;
+    case 5: k_batch_direct<2, 256, 256><<<b, 256, 0, st>>>(t); break;
+    case 6: k_batch_direct<4, 128, 256><<<b, 128, 0, st>>>(t); break;
+    default: k_batch_direct<4, 256, 256><<<b, 256, 0, st>>>(t); break;
+    }
+    return cudaGetLastError();
+}
+
+template <int kMethod>
+static cudaError_t launch_batch_force_m(const BatchTables &t, int comp, int quad, int sm_count, cudaStream_t st) {
+    const void *fn;
+    if (quad) fn = comp ? (const void *)k_batch_force<kMethod, true, true> : (const void *)k_batch_force<kMethod, false, true>;
+    else fn = comp ? (const void *)k_batch_force<kMethod, true, false> : (const void *)k_batch_force<kMethod, false, false>;
+    int blocks = resident(fn, kForceThreads, sm_count);
+    const int need = (t.groups + kForceWarps - 1) / kForceWarps;
+    if (blocks > need) blocks = need > 0 ? need : 1;
+    if (quad) {
+        if (comp) k_batch_force<kMethod, true, true><<<blocks, kForceThreads, 0, st>>>(t);
+        else k_batch_force<kMethod, false, true><<<blocks, kForceThreads, 0, st>>>(t);
+    } else {
+        if (comp) k_batch_force<kMethod, true, false><<<blocks, kForceThreads, 0, st>>>(t);
+        else k_batch_force<kMethod, false, false><<<blocks, kForceThreads, 0, st>>>(t);
+    }
+    return cudaGetLastError();
+}
+
+// One batched step.  Kernels with no work in this batch are not launched.
+// Returns the number of kernels launched through *launches.
+cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int quad, int direct_variant,
+                              int sm_count, cudaStream_t st, int *launches) {
+    int nl = 0;
+    cudaError_t e = cudaSuccess;
+    const int sb = (t.nsys + 127) / 128;
+    if (t.chunks > 0) {
+        k_batch_reset<<<sb, 128, 0, st>>>(t);
+        k_batch_bbox<<<t.chunks, 256, 0, st>>>(t);
+        k_batch_build<<<t.chunks, 256, 0, st>>>(t);
+        int sblocks = sm_count * 8;
+        const int need = (t.cells + 255) / 256;
+        if (sblocks > need) sblocks = need;
+        k_batch_summarize<<<sblocks, 256, 0, st>>>(t);
+        int rblocks = resident((const void *)k_batch_sort, 256, sm_count);
+        if (rblocks > need) rblocks = need;
+        k_batch_sort<<<rblocks, 256, 0, st>>>(t);
+        if ((e = cudaMemsetAsync(t.work, 0, sizeof(int), st)) != cudaSuccess) return e;
+        switch (method) {
+        case 1: e = launch_batch_force_m<1>(t, comp, quad, sm_count, st); break;
+        case 2: e = launch_batch_force_m<2>(t, comp, quad, sm_count, st); break;
+        case 3: e = launch_batch_force_m<3>(t, comp, quad, sm_count, st); break;
+        default: e = launch_batch_force_m<0>(t, comp, quad, sm_count, st); break;
+        }
+        if (e != cudaSuccess) return e;
+        nl += 6;
+    }
+    if (t.dblocks > 0) {
+        if ((e = launch_direct_variant(t, direct_variant, st)) != cudaSuccess) return e;
+        nl += 1;
+    }
+    k_batch_flip<<<sb, 128, 0, st>>>(t);
+    nl += 1;
+    if (launches) *launches = nl;
+    return cudaGetLastError();
+}
+
+__global__ void k_batch_clear(BatchTables t) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= t.nsys) return;
+    Ctrl *c = t.sys[k].v.ctrl;
+    c->status = 0;
+    c->status_info = 0;
+    c->interactions = 0;
+    c->opened = 0;
+    c->cell_interactions = 0;
+}
+
+cudaError_t launch_batch_clear(const BatchTables &t, cudaStream_t st) {
+    k_batch_clear<<<(t.nsys + 127) / 128, 128, 0, st>>>(t);
+    return cudaGetLastError();
+}
+
+// The direct-sum kernel alone, for the autotuner.
+cudaError_t launch_batch_direct_only(const BatchTables &t, int variant, cudaStream_t st) {
+    if (t.dblocks <= 0) return cudaSuccess;
+    return launch_direct_variant(t, variant, st);
+}
+
+}  // namespace nbgb

@@ -6,11 +6,7 @@
 // saturate_tree (kernels/saturate_tree.cl) and the empty sort
 // (kernels/sort.cl).  Each is re-designed for sm_103a; the differences that
 // change results are listed at each kernel.
-#include <cooperative_groups.h>
-
-#include "nbgb_internal.cuh"
-
-namespace cg = cooperative_groups;
+#include "bh_device.cuh"
 
 namespace nbgb {
 
@@ -83,154 +79,20 @@ __global__ void __launch_bounds__(256) k_bbox(const float4 *__restrict__ b, int 
 }
 
 // ---------------------------------------------------------------------------
-// Geometry of the build.  Both policies keep `g` = the region of the slot the
-// body is about to enter, so the split can give a new cell that region.
-// ---------------------------------------------------------------------------
-struct GeoCube {  // Burtscher: cubic root, child centre = centre -/+ r/2
-    float cx, cy, cz, r;
-    __device__ __forceinline__ int octant(float x, float y, float z) const {
-        return (y < cy ? 4 : 0) + (x < cx ? 2 : 0) + (z < cz ? 1 : 0);
-    }
-    __device__ __forceinline__ void descend(float x, float y, float z) {
-        r = __fmul_rn(r, 0.5f);
-        cx = __fadd_rn(cx, x < cx ? -r : r);
-        cy = __fadd_rn(cy, y < cy ? -r : r);
-        cz = __fadd_rn(cz, z < cz ? -r : r);
-    }
-};
-
-struct RefBox {  // the reference: calculateOctantIdx / adjustBoundaryValues
-    float mnx, mny, mnz, mxx, mxy, mxz;
-    // build_tree.hcl:14-29 -- 4*(dy<0) + 2*(dx<0) + (dz<0), centre (max+min)/2
-    __device__ __forceinline__ int octant(float x, float y, float z) const {
-        const float cx = __fmul_rn(__fadd_rn(mxx, mnx), 0.5f);
-        const float cy = __fmul_rn(__fadd_rn(mxy, mny), 0.5f);
-        const float cz = __fmul_rn(__fadd_rn(mxz, mnz), 0.5f);
-        return (y < cy ? 4 : 0) + (x < cx ? 2 : 0) + (z < cz ? 1 : 0);
-    }
-    // build_tree.hcl:31-54, y bounds following the x difference (:42-46)
-    __device__ __forceinline__ void descend(float x, float y, float z) {
-        const float cx = __fmul_rn(__fadd_rn(mxx, mnx), 0.5f);
-        const float cy = __fmul_rn(__fadd_rn(mxy, mny), 0.5f);
-        const float cz = __fmul_rn(__fadd_rn(mxz, mnz), 0.5f);
-        if (x > cx) mnx = cx; else mxx = cx;
-        if (x > cx) mny = cy; else mxy = cy;
-        if (z > cz) mnz = cz; else mxz = cz;
-        (void)y;
-    }
-};
-
-// ---------------------------------------------------------------------------
-// build: concurrent octree insertion with atomicCAS child locks (Burtscher;
-// kernels/build_tree.cl:42-161).  Empty slot: CAS(-1 -> body).  Slot holding
-// a body: CAS(body -> LOCKED), grow a chain of cells until the two bodies
-// separate, publish the chain with one release store of its top cell.
-// Cells come from one downward counter with warp-aggregated atomicSub (one
-// atomic per converged group of splitting threads).  A fresh cell's eight
-// slots, parent link, arrival counter and sort start are initialised by the
-// allocating thread before publication.  Every retry loop is bounded
-// (kSpinCap) and watches the status word; a cell overflow or an over-deep
-// chain restores the locked slot, records the status and leaves.
-//
-// Reference semantics (kRef): the first probe is slot 0 of the super-root
-// without an octant test (build_tree.cl:57-65); the root region is the
-// bounding box; boxes halve as adjustBoundaryValues does.
+// build: one body per thread, grid-stride (insert_body, bh_device.cuh).
 // ---------------------------------------------------------------------------
 template <class Geo, bool kRef>
 __global__ void __launch_bounds__(256) k_build(DevSim s) {
     Ctrl *ctrl = s.ctrl;
     if (read_status(ctrl)) return;
-    const int n = s.n, root = n + s.cap;
     float box[6];
     load_box(ctrl, box);
-    Geo root_g;
-    if constexpr (kRef) {
-        root_g = Geo{box[0], box[1], box[2], box[3], box[4], box[5]};
-    } else {
-        const float ex = box[3] - box[0], ey = box[4] - box[1], ez = box[5] - box[2];
-        float m = ex > ey ? ex : ey;
-        m = m > ez ? m : ez;
-        root_g = Geo{__fmul_rn(__fadd_rn(box[0], box[3]), 0.5f), __fmul_rn(__fadd_rn(box[1], box[4]), 0.5f),
-                     __fmul_rn(__fadd_rn(box[2], box[5]), 0.5f), __fmul_rn(0.5f, m)};
-    }
+    const Geo root_g = Geo::root(box);
     int local_max = 0;
     const int stride = gridDim.x * blockDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float4 P = s.body_cur[i];
-        Geo g = root_g;
-        int node = root, slot, depth = 0;
-        if constexpr (kRef) {
-            slot = 0;
-        } else {
-            slot = g.octant(P.x, P.y, P.z);
-            g.descend(P.x, P.y, P.z);
-        }
-        int *cslot = &s.child[(node - n) * 8 + slot];
-        int ch = ld_volatile(cslot);
-        long long spins = 0;
-        while (true) {
-            while (ch >= n) {  // descend through published cells
-                node = ch;
-                slot = g.octant(P.x, P.y, P.z);
-                g.descend(P.x, P.y, P.z);
-                ++depth;
-                cslot = &s.child[(node - n) * 8 + slot];
-                ch = ld_volatile(cslot);
-            }
-            if (ch == kEmpty) {
-                if (atomicCAS(cslot, kEmpty, i) == kEmpty) break;
-            } else if (ch >= 0) {
-                if (atomicCAS(cslot, ch, kLocked) == ch) {
-                    const int og = ch;
-                    const float4 O = s.body_cur[og];
-                    Geo og_g = g;
-                    int patch = -1, link_node = node, link_slot = slot, c2;
-                    int fail = 0;
-                    do {
-                        cg::coalesced_group grp = cg::coalesced_threads();
-                        int base = 0;
-                        if (grp.thread_rank() == 0) base = atomicSub(&ctrl->bottom, (int)grp.size());
-                        base = grp.shfl(base, 0);
-                        const int cell = base - 1 - (int)grp.thread_rank();
-                        ++depth;
-                        if (cell < n) { fail = kStCellOverflow; break; }
-                        if (depth > 2 * kMaxDepth) { fail = kStDepth; break; }
-                        patch = max(patch, cell);
-                        const int c = cell - n;
-                        int4 *row = reinterpret_cast<int4 *>(&s.child[c * 8]);
-                        row[0] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
-                        row[1] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
-                        s.parent[c] = link_node;
-                        s.arrive[c] = 0;
-                        s.start[c] = -1;
-                        if (patch != cell) s.child[(link_node - n) * 8 + link_slot] = cell;
-                        const int oslot = og_g.octant(O.x, O.y, O.z);
-                        og_g.descend(O.x, O.y, O.z);
-                        s.child[c * 8 + oslot] = og;
-                        slot = g.octant(P.x, P.y, P.z);
-                        g.descend(P.x, P.y, P.z);
-                        link_node = cell;
-                        link_slot = slot;
-                        c2 = (slot == oslot) ? og : kEmpty;
-                    } while (c2 >= 0);
-                    if (fail) {
-                        st_volatile(cslot, og);  // release the lock unchanged
-                        set_status(ctrl, fail, i);
-                        return;
-                    }
-                    s.child[(link_node - n) * 8 + link_slot] = i;
-                    __threadfence();
-                    st_volatile(cslot, patch);  // publish the chain
-                    break;
-                }
-            }
-            if (++spins > kSpinCap) {
-                set_status(ctrl, kStSpinTimeout, i);
-                return;
-            }
-            if ((spins & 1023) == 0 && read_status(ctrl)) return;
-            ch = ld_volatile(cslot);
-        }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += stride) {
+        const int depth = insert_body<Geo, kRef>(s, root_g, i);
+        if (depth < 0) return;
         local_max = max(local_max, depth);
     }
     const unsigned am = __activemask();
@@ -238,191 +100,34 @@ __global__ void __launch_bounds__(256) k_build(DevSim s) {
     if ((threadIdx.x & 31) == __ffs(am) - 1) atomicMax(&ctrl->max_depth, wmax);
 }
 
-__device__ __forceinline__ void load_children(const int *child, int c, int chs[8], int &nch, int &nbody, int n) {
-    const int4 a0 = *reinterpret_cast<const int4 *>(&child[c * 8]);
-    const int4 a1 = *reinterpret_cast<const int4 *>(&child[c * 8 + 4]);
-    chs[0] = a0.x; chs[1] = a0.y; chs[2] = a0.z; chs[3] = a0.w;
-    chs[4] = a1.x; chs[5] = a1.y; chs[6] = a1.z; chs[7] = a1.w;
-    nch = 0;
-    nbody = 0;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        nch += chs[j] >= 0;
-        nbody += (chs[j] >= 0) & (chs[j] < n);
-    }
-}
-
 // ---------------------------------------------------------------------------
-// summarize: bottom-up centre of mass with L2-resident arrival counters.  One
-// thread per cell adds the number of the cell's body children to the cell's
-// counter in one atomic; a completed child cell adds one.  Whoever brings the
-// counter to the number of children computes the cell and then arrives at
-// the parent, and so on up to the root.  No thread ever waits, so no
-// co-residency of the grid is needed (saturate_tree.cl spins on child
-// masses, :96-117).  The completing thread sums the children in slot order
-// -- mass += m, centre += x*m, centre *= 1/mass, each rounded separately
-// (saturate_tree.cl:84-87,129-133) -- so the result does not depend on the
-// schedule and matches the oracle bit for bit.  It also writes the compacted
-// child list and the packed child {x,y,z,m} line the force walk reads (the
-// reference compacts in place, saturate_tree.cl:57-63, and skips the move
-// when a child's index equals its new slot number; that defect is not
-// reproduced).  Fences: release before every counter update, acquire after
-// the update that completes a cell; child-cell data written in this kernel is
-// read through L2 (__ldcg).
+// summarize: one cell of [bottom, root] per thread (summarize_from).
 // ---------------------------------------------------------------------------
 template <bool kQuad>
 __global__ void __launch_bounds__(256) k_summarize(DevSim s) {
     if (read_status(s.ctrl)) return;
-    const int n = s.n, root = n + s.cap;
+    const int root = s.n + s.cap;
     const int bottom = s.ctrl->bottom;
     const int stride = gridDim.x * blockDim.x;
-    for (int k = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); k <= root; k += stride) {
-        int node = k;
-        int chs[8], nch, nbody;
-        load_children(s.child, node - n, chs, nch, nbody, n);
-        if (nbody == 0) continue;  // completed by its child cells
-        if (nbody != nch) {
-            const int old = atomicAdd(&s.arrive[node - n], nbody);
-            if (old + nbody != nch) continue;
-            __threadfence();
-        }
-        while (true) {
-            const int c = node - n;
-            float M = 0.0f, cx = 0.0f, cy = 0.0f, cz = 0.0f;
-            int cnt = 0, w = 0;
-            int wc[8];
-            float4 wp[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                wc[j] = kEmpty;
-                wp[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            }
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int ch = chs[j];
-                if (ch < 0) continue;
-                float4 pm;
-                int cc;
-                if (ch < n) {
-                    pm = s.body_cur[ch];
-                    cc = 1;
-                } else {
-                    pm = __ldcg(&s.cell_pm[ch - n]);
-                    cc = __ldcg(&s.count[ch - n]);
-                }
-                M = __fadd_rn(M, pm.w);
-                cx = __fadd_rn(cx, __fmul_rn(pm.x, pm.w));
-                cy = __fadd_rn(cy, __fmul_rn(pm.y, pm.w));
-                cz = __fadd_rn(cz, __fmul_rn(pm.z, pm.w));
-                cnt += cc;
-                // w <= j, so a static index write through a select chain
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (q == w) { wc[q] = ch; wp[q] = pm; }
-                ++w;
-            }
-            int4 *wrow = reinterpret_cast<int4 *>(&s.wchild[c * 8]);
-            wrow[0] = make_int4(wc[0], wc[1], wc[2], wc[3]);
-            wrow[1] = make_int4(wc[4], wc[5], wc[6], wc[7]);
-            float4 *prow = &s.wpm[c * 8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) prow[q] = wp[q];
-            const float inv = __frcp_rn(M);
-            const float X = __fmul_rn(cx, inv), Y = __fmul_rn(cy, inv), Z = __fmul_rn(cz, inv);
-            s.count[c] = cnt;
-            s.cell_pm[c] = make_float4(X, Y, Z, M);
-            if constexpr (kQuad) {
-                // traceless quadrupole about the centre of mass, children in
-                // slot order: Q += Q_child + m (3 d d^T - |d|^2 I), d = x_child - X
-                float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f, q3 = 0.0f, q4 = 0.0f, q5 = 0.0f;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int ch = wc[j];
-                    if (ch < 0) break;
-                    const float4 pm = wp[j];
-                    float4 oa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    float4 ob = oa;
-                    if (ch >= n) {
-                        oa = __ldcg(&s.cell_q[2 * (ch - n)]);
-                        ob = __ldcg(&s.cell_q[2 * (ch - n) + 1]);
-                    }
-                    s.wqa[c * 8 + j] = oa;
-                    s.wqb[c * 8 + j] = make_float2(ob.x, ob.y);
-                    const float m = pm.w;
-                    const float dx = __fsub_rn(pm.x, X), dy = __fsub_rn(pm.y, Y), dz = __fsub_rn(pm.z, Z);
-                    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                    const float tx = __fmul_rn(3.0f, dx), ty = __fmul_rn(3.0f, dy);
-                    q0 = __fadd_rn(q0, __fmaf_rn(m, __fmaf_rn(tx, dx, -r2), oa.x));
-                    q1 = __fadd_rn(q1, __fmaf_rn(m, __fmaf_rn(ty, dy, -r2), oa.y));
-                    q2 = __fadd_rn(q2, __fmaf_rn(m, __fmaf_rn(__fmul_rn(3.0f, dz), dz, -r2), oa.z));
-                    q3 = __fadd_rn(q3, __fmaf_rn(m, __fmul_rn(tx, dy), oa.w));
-                    q4 = __fadd_rn(q4, __fmaf_rn(m, __fmul_rn(tx, dz), ob.x));
-                    q5 = __fadd_rn(q5, __fmaf_rn(m, __fmul_rn(ty, dz), ob.y));
-                }
-                s.cell_q[2 * c] = make_float4(q0, q1, q2, q3);
-                s.cell_q[2 * c + 1] = make_float4(q4, q5, 0.0f, 0.0f);
-            }
-            if (node == root) break;
-            const int p = s.parent[c];
-            load_children(s.child, p - n, chs, nch, nbody, n);
-            __threadfence();
-            const int old = atomicAdd(&s.arrive[p - n], 1);
-            if (old + 1 != nch) break;
-            __threadfence();
-            node = p;
-        }
-    }
+    for (int k = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); k <= root; k += stride)
+        summarize_from<kQuad>(s, k);
 }
 
 // ---------------------------------------------------------------------------
-// sort: in-order body placement from subtree counts (Burtscher's sort; the
-// reference's kernels/sort.cl is empty).  Cells are visited from the root
-// downward (descending index: a parent was allocated before its children);
-// a cell waits -- bounded -- until its parent has published its start, then
-// hands each child cell a start (running sum of counts in slot order) and
-// places each child body.  The result is the depth-first listing of bodies
-// in slot order, which the oracle's orc_sort reproduces exactly.  Launched
-// on a grid no larger than what is co-resident.
+// sort: cells visited from the root downward (descending index: a parent was
+// allocated before its children), so every wait in sort_cell is for a cell
+// handled earlier; launched on a grid no larger than what is co-resident.
+// The result is the depth-first listing of bodies in slot order, which the
+// oracle's orc_sort reproduces exactly.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_sort(DevSim s) {
     Ctrl *ctrl = s.ctrl;
     if (read_status(ctrl)) return;
-    const int n = s.n, root = n + s.cap;
+    const int root = s.n + s.cap;
     const int bottom = ctrl->bottom;
     const int stride = gridDim.x * blockDim.x;
-    for (int k = root - (int)(blockIdx.x * blockDim.x + threadIdx.x); k >= bottom; k -= stride) {
-        const int c = k - n;
-        int st = ld_volatile(&s.start[c]);
-        long long spins = 0;
-        while (st < 0) {
-            if (++spins > kSpinCap) {
-                set_status(ctrl, kStSpinTimeout, k);
-                return;
-            }
-            if ((spins & 1023) == 0 && read_status(ctrl)) return;
-            __nanosleep(32);
-            st = ld_volatile(&s.start[c]);
-        }
-        const int4 a0 = *reinterpret_cast<const int4 *>(&s.wchild[c * 8]);
-        const int4 a1 = *reinterpret_cast<const int4 *>(&s.wchild[c * 8 + 4]);
-        const int chs[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int ch = chs[j];
-            if (ch < 0) break;
-            if (ch >= n) {
-                st_volatile(&s.start[ch - n], st);
-                st += s.count[ch - n];
-            } else {
-                if ((unsigned)st >= (unsigned)n) {  // inconsistent counts: never write past sorted[]
-                    set_status(ctrl, kStSpinTimeout, st);
-                    return;
-                }
-                s.sorted[st] = ch;
-                ++st;
-            }
-        }
-    }
+    for (int k = root - (int)(blockIdx.x * blockDim.x + threadIdx.x); k >= bottom; k -= stride)
+        if (!sort_cell(s, k)) return;
 }
 
 // ---------------------------------------------------------------------------

@@ -38,7 +38,9 @@ struct Ctrl {
     int bottom;            // lowest allocated cell index
     int max_depth;
     int work;              // dynamic work counter of the force pass
-    int pad0;
+    int parity;            // batched systems: which body buffer is current
+    int kdk_primed;        // batched systems: a KDK half-kick has happened
+    int pad0[3];
     // cleared by the host once per nb_step call (everything from here on)
     int status;
     int status_info;
@@ -124,6 +126,49 @@ __device__ __forceinline__ void load_box(const Ctrl *c, float box[6]) {
     for (int k = 0; k < 6; ++k) box[k] = key2f(c->bbox_key[k]);
 }
 
+// One system of a batch (nb_batch / nb_server): its buffers, its step
+// parameters and where its work starts in the batch-wide index spaces.
+enum SysKind { kSysBH = 0, kSysDirect = 1 };
+struct SysDesc {
+    DevSim v;          // pointers; body_cur / body_next come from body[] and ctrl->parity
+    float4 *body[2];
+    StepParams p;      // theta, eps, G, dt, method, tree_ref, crit_ref, quadrupole
+    int kind;          // SysKind
+    int active;        // 0: skipped by every stage
+    int body_begin;    // prefix over all systems' bodies
+    int chunk_begin;   // prefix over BH systems' bbox/build chunks
+    int cell_begin;    // prefix over BH systems' cell slots (cap + 1)
+    int group_begin;   // prefix over BH systems' warp groups
+    int dblock_begin;  // prefix over direct systems' target blocks
+};
+
+// Prefix tables (nsys + 1 entries each) and totals of a batch.
+struct BatchTables {
+    const SysDesc *sys;
+    int nsys;
+    const int *chunk_prefix, *cell_prefix, *group_prefix, *dblock_prefix;
+    int chunks, cells, groups, dblocks;
+    int *work;  // batch-wide force work counter
+};
+
+__device__ __forceinline__ int find_system(const int *prefix, int nsys, int x) {
+    int lo = 0, hi = nsys;  // largest k with prefix[k] <= x and prefix[k+1] > x
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&prefix[mid]) <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ DevSim system_view(const SysDesc &d) {
+    DevSim v = d.v;
+    const int par = ld_volatile(&v.ctrl->parity) & 1;
+    v.body_cur = d.body[par];
+    v.body_next = d.body[par ^ 1];
+    return v;
+}
+
 // Launch helpers implemented in the kernel translation units.
 struct LaunchShape {
     int blocks;
@@ -150,5 +195,15 @@ cudaError_t launch_force_probe(const float4 *body, int n, const int *sample, int
                                double *out3, cudaStream_t st);
 cudaError_t launch_diagnostics(const float4 *body, const float4 *vel, int n, int with_potential, double eps,
                                double G, double *out9, cudaStream_t st);
+
+// batched systems (k_batch.cu)
+constexpr int kBatchChunk = 4096;  // bodies per bbox / build block
+int batch_direct_variants();
+int batch_direct_block_bodies(int variant);
+cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int quad, int direct_variant,
+                              int sm_count, cudaStream_t st, int *launches);
+cudaError_t launch_batch_direct_only(const BatchTables &t, int variant, cudaStream_t st);
+// clears the status word and work counters of every system (once per call)
+cudaError_t launch_batch_clear(const BatchTables &t, cudaStream_t st);
 
 }  // namespace nbgb
