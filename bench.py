@@ -42,6 +42,7 @@ WORKLOAD = dict(name="bh_plummer_n4m_theta0.5", n=4194304, sigma=(1.0, 1.0, 0.2)
 PROBE_SAMPLES = 8192
 FP32_LANES_PER_SM = 128
 FLOPS_PER_INTERACTION = 12  # FP32 ops per monopole interaction (3 sub, 3 fma, 3 mul, 3 fma)
+FORCE_DRAM_BYTES_PER_BODY = (386.390528e6 + 75.163648e6) / 1048576  # dram read + write, k_force, N = 1M
 FLOPS_PER_QUADRUPOLE = 19   # extra FP32 ops per cell quadrupole term (Q.d 9, d.Q.d 3, r^5 r^7 2, 2.5*sq 1, 4 fma)
 
 
@@ -310,12 +311,9 @@ def run_ours(args, dist: Dist):
     inter_per_step = inter / args.steps
     flops_per_step = (FLOPS_PER_INTERACTION * inter + FLOPS_PER_QUADRUPOLE * cell_inter) / args.steps
     fp32_peak_ops = FP32_LANES_PER_SM * sm_count * sm_mhz * 1e6  # one FP32 op per lane per clock
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "force_traffic.json")
-    if os.path.exists(tfile):
-        with open(tfile) as f:
-            t = json.load(f)
-        traffic = t["bytes_per_body"] * n
+    # DRAM bytes of one force launch from the ncu capture at N = 1M
+    # (profiles/k_force_bh_n1m_theta0.5_quadrupole.md), scaled by bodies
+    traffic = FORCE_DRAM_BYTES_PER_BODY * n
     out = {
         "metric": "BH body-updates/s N=4M theta=0.5 (RMS force err <= 1e-3)",
         "value": value,
@@ -405,6 +403,134 @@ def run_reference(args, dist: Dist):
     }
 
 
+# ---------------------------------------------------------------------------
+# batched systems vs a loop of plain solves
+# ---------------------------------------------------------------------------
+BATCH = dict(name="batch512_loguniform_1k_256k", systems=512, n_min=1024, n_max=262144, direct_below=8192,
+             theta=0.5, eps=0.01, dt=1e-3, G=1.0, seed=0, steps=100, plain_steps=5)
+
+
+def batch_configs(nb, systems=BATCH["systems"], seed=BATCH["seed"]):
+    """Seeded systems: N log-uniform in [1024, 262144]; even systems normal(0,1)
+    at rest, odd systems uniform in the unit ball with circular velocities
+    about z; masses 1/N; N < 8192 direct sum, the rest Barnes-Hut."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(BATCH["n_min"]), np.log(BATCH["n_max"]), size=systems)).astype(np.int64)
+    cfgs = []
+    for k, n in enumerate(ns):
+        ball = k % 2 == 1
+        cfgs.append(nb.default_config(
+            num_of_bodies=int(n), algo_config=nb.BARNES_HUT if n >= BATCH["direct_below"] else nb.BRUTE_FORCE_LOCAL,
+            theta=BATCH["theta"], epsilon=BATCH["eps"], direct_epsilon=BATCH["eps"],
+            gravitational_constant=BATCH["G"], numerical_method=nb.EULER,
+            pos_config=nb.BALL_POS if ball else nb.NORMAL_SIGMA_POS, pos_sigma=(1.0, 1.0, 1.0),
+            starting_volume_radius=1.0, vel_config=nb.CIRCULAR_Z_VEL if ball else nb.FUNC_ZERO_VEL,
+            mass_config=nb.MASS_EQUAL, seed=seed * 100003 + k))
+    return cfgs
+
+
+def run_batch(args, dist: Dist):
+    from nbodysimulation_gb300 import build as nbbuild
+    if dist.local_rank == 0:
+        nbbuild.build()
+    dist.barrier()
+    import nbodysimulation_gb300 as nb
+    dev = dist.local_rank
+    dt = BATCH["dt"]
+    cfgs = batch_configs(nb, args.systems, BATCH["seed"] + dist.rank)
+    for c in cfgs:
+        c.device = dev
+    states = [nb.generate_ic(c) for c in cfgs]
+    ns = np.array([c.num_of_bodies for c in cfgs], np.int64)
+    bodies = int(ns.sum())
+    n_bh = int(sum(1 for c in cfgs if c.algo_config == nb.BARNES_HUT))
+
+    # --- batched: one graph per step over all systems ---
+    b = nb.Batch(cfgs)
+    for k, (p, v, m) in enumerate(states):
+        b.set_state(k, p, m, v)
+    cache = os.path.join(ROOT, "nbodysimulation_gb300", "_build", "autotune.json")
+    variant = b.autotune(cache)
+    b.step(dt, args.warmup)
+    steps = args.batch_steps
+    clocks = ClockSampler(dev)
+    dist.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    ms = b.time_steps(dt, steps)
+    clk = clocks.stop()
+    t0 = time.perf_counter()
+    b.step(dt, steps)
+    wall_b = time.perf_counter() - t0
+    dist.barrier()
+    info = b.info()
+    # end to end: the states go up from the host, `steps` steps, the
+    # positions come back
+    t0 = time.perf_counter()
+    for k, (p, v, m) in enumerate(states):
+        b.set_state(k, p, m, v)
+    b.step(dt, steps)
+    for k in range(len(cfgs)):
+        b.get_state(k)
+    e2e_b = time.perf_counter() - t0
+    b.close()
+    ms = dist.max(ms)
+    wall_b = dist.max(wall_b)
+    e2e_b = dist.max(e2e_b)
+    total = dist.sum(float(bodies))
+    batched = total * steps / (ms / 1e3)
+    batched_wall = total * steps / wall_b
+
+    # --- plain: one standalone handle at a time, nb_step per system ---
+    pk = args.plain_steps
+    wall_p = 0.0
+    dev_p = 0.0
+    for c, (p, v, m) in zip(cfgs, states):
+        with nb.Simulation(c) as s:
+            s.set_state(p, m, v)
+            s.step(dt, 1)
+            t0 = time.perf_counter()
+            s.step(dt, pk)
+            wall_p += time.perf_counter() - t0
+            dev_p += s.time_steps(dt, pk)
+    wall_p = dist.max(wall_p)
+    dev_p = dist.max(dev_p)
+    plain_wall = total * pk / wall_p
+    plain_dev = total * pk / (dev_p / 1e3)
+    if dist.rank != 0:
+        return None
+    return {
+        "metric": "batched body-updates/s, 512 systems N log-uniform 1k-256k (vs a loop of plain solves)",
+        "value": batched,
+        "unit": "body-updates/s",
+        "n_gpus": dist.world,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded: normal(0,1) at rest / unit ball with circular z velocities, masses 1/N)",
+        "config": {"workload": BATCH["name"], "systems": len(cfgs), "bodies": bodies, "tree_systems": n_bh,
+                   "direct_systems": len(cfgs) - n_bh, "direct_below": BATCH["direct_below"],
+                   "theta": BATCH["theta"], "eps": BATCH["eps"], "dt": dt, "G": BATCH["G"], "integrator": "euler",
+                   "precision": "fp32", "multipole": "monopole", "direct_variant": variant,
+                   "launches_per_step": info["launches_per_step"],
+                   "l2": "inputs larger than L2 (all systems' bodies and trees, several GB)",
+                   "parallelism": f"replicas x{dist.world}"},
+        "batched_wall": batched_wall,
+        "plain": {"value_wall": plain_wall, "value_device": plain_dev, "steps_per_system": pk,
+                  "how": "one nb_create handle per system, nb_step(dt, k) per system in turn"},
+        "batched_over_plain_wall": batched_wall / plain_wall,
+        "e2e": {"value": total * steps / e2e_b, "unit": "body-updates/s",
+                "h2d_bytes_per_step": 28 * bodies / steps, "d2h_bytes_per_step": 48 * bodies / steps,
+                "how": "all states up once, steps steps, all states down once; bytes amortised per step"},
+        "gpu_launches": info["launches_per_step"] * steps,
+        "clocks": clk,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -415,12 +541,22 @@ def main():
                     help="bodies per system (default the 4M workload; smaller sizes for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
     ap.add_argument("--skip-fp32", action="store_true", help="omit the plain-FP32 accumulation run")
+    ap.add_argument("--mode", choices=("step", "batch"), default="step",
+                    help="step: the 4M Barnes-Hut system; batch: 512 batched systems vs plain solves")
+    ap.add_argument("--systems", type=int, default=BATCH["systems"])
+    ap.add_argument("--batch-steps", type=int, default=BATCH["steps"])
+    ap.add_argument("--plain-steps", type=int, default=BATCH["plain_steps"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     dist = Dist()
     try:
-        out = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+        if args.impl == "reference":
+            out = run_reference(args, dist)
+        elif args.mode == "batch":
+            out = run_batch(args, dist)
+        else:
+            out = run_ours(args, dist)
         if dist.rank == 0 and out is not None:
             print(json.dumps(out), flush=True)
     finally:
