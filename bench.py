@@ -531,6 +531,156 @@ def run_batch(args, dist: Dist):
     }
 
 
+# ---------------------------------------------------------------------------
+# serving: a Poisson job stream through the job server vs plain solves
+# ---------------------------------------------------------------------------
+SERVE = dict(name="serve_poisson200_n1k_1m", rate=200.0, seconds=2.0, n_min=1024, n_max=1048576, steps_min=10,
+             steps_max=500, thetas=(0.5, 0.7), eps=0.01, dt=1e-3, G=1.0, direct_below=8192, budget=120e9,
+             snapshot_every=10, seed=0)
+
+
+def serve_jobs(nb, rate, seconds, seed):
+    """Seeded job stream: Poisson arrivals; N log-uniform in [1024, 2^20];
+    steps uniform in [10, 500]; normal(0,1) or unit-ball initial conditions
+    50/50 (the ball with circular velocities about z); masses 1/N; theta 0.5
+    or 0.7; N < 8192 direct sum, the rest Barnes-Hut."""
+    rng = np.random.default_rng(seed)
+    jobs, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        n = int(np.exp(rng.uniform(np.log(SERVE["n_min"]), np.log(SERVE["n_max"]))))
+        steps = int(rng.integers(SERVE["steps_min"], SERVE["steps_max"] + 1))
+        ball = bool(rng.integers(0, 2))
+        theta = float(rng.choice(SERVE["thetas"]))
+        cfg = nb.default_config(
+            num_of_bodies=n, algo_config=nb.BARNES_HUT if n >= SERVE["direct_below"] else nb.BRUTE_FORCE_LOCAL,
+            theta=theta, epsilon=SERVE["eps"], direct_epsilon=SERVE["eps"], gravitational_constant=SERVE["G"],
+            numerical_method=nb.EULER, pos_config=nb.BALL_POS if ball else nb.NORMAL_SIGMA_POS,
+            pos_sigma=(1.0, 1.0, 1.0), starting_volume_radius=1.0,
+            vel_config=nb.CIRCULAR_Z_VEL if ball else nb.FUNC_ZERO_VEL, mass_config=nb.MASS_EQUAL,
+            seed=seed * 1000003 + len(jobs))
+        jobs.append((t, cfg, steps))
+    return jobs
+
+
+def run_serve_arm(nb, jobs, dt, dev):
+    """The job server: a client thread submits each job at its arrival time
+    (initial conditions generated by the server); snapshots and results come
+    back through the callback."""
+    counts = {"snapshots": 0, "snapshot_bytes": 0, "done": 0}
+    lock = threading.Lock()
+
+    def on_event(job, event, value, pos, vel):
+        with lock:
+            if event == nb.JOB_EVENT_SNAPSHOT:
+                counts["snapshots"] += 1
+            elif event == nb.JOB_EVENT_DONE:
+                counts["done"] += 1
+
+    srv = nb.Server(on_event=on_event, copy_arrays=False, device=dev, hbm_budget_bytes=int(SERVE["budget"]),
+                    snapshot_every=SERVE["snapshot_every"])
+    sizes = {}
+    t0 = time.perf_counter()
+    for t, cfg, steps in jobs:
+        delay = t - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        cfg.device = dev
+        j = srv.submit(cfg, steps, dt)
+        sizes[j] = cfg.num_of_bodies
+    st_wait = srv.wait(-1, 3600.0)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    if st_wait != 0 or st["failed"]:
+        raise RuntimeError(f"serving run failed: status {st_wait}, {st['failed']} failed jobs")
+    span = st["last_done_s"] - st["first_submit_s"]
+    return {"value": st["body_updates"] / span, "latency_p50_s": st["latency_p50_s"],
+            "latency_p99_s": st["latency_p99_s"], "latency_max_s": st["latency_max_s"],
+            "latency_mean_s": st["latency_mean_s"], "jobs": st["completed"], "rounds": st["rounds"],
+            "peak_jobs_on_gpu": st["peak_jobs"], "peak_bytes": st["peak_bytes"], "span_s": span,
+            "snapshots": counts["snapshots"], "wall_s": wall, "body_updates": st["body_updates"]}
+
+
+def run_plain_arm(nb, jobs, dt, dev):
+    """One job at a time in arrival order through a standalone handle:
+    initial conditions, nb_set_state, nb_step in rounds of 10 with the
+    positions read back after each round (the snapshots), final state."""
+    lat = []
+    total = 0.0
+    t0 = time.perf_counter()
+    for t, cfg, steps in jobs:
+        now = time.perf_counter() - t0
+        if now < t:
+            time.sleep(t - now)
+        cfg.device = dev
+        pos, vel, mass = nb.generate_ic(cfg)
+        with nb.Simulation(cfg) as s:
+            s.set_state(pos, mass, vel)
+            done = 0
+            while done < steps:
+                k = min(SERVE["snapshot_every"], steps - done)
+                s.step(dt, k)
+                done += k
+                s.get_state()
+        lat.append(time.perf_counter() - t0 - t)
+        total += cfg.num_of_bodies * steps
+    span = time.perf_counter() - t0 - jobs[0][0]
+    lat = np.sort(np.array(lat))
+    pick = lambda p: float(lat[min(len(lat) - 1, max(0, int(np.ceil(p / 100 * len(lat))) - 1))])
+    return {"value": total / span, "latency_p50_s": pick(50), "latency_p99_s": pick(99),
+            "latency_max_s": float(lat[-1]), "jobs": len(jobs), "span_s": span, "body_updates": total}
+
+
+def run_serve(args, dist: Dist):
+    from nbodysimulation_gb300 import build as nbbuild
+    if dist.local_rank == 0:
+        nbbuild.build()
+    dist.barrier()
+    import nbodysimulation_gb300 as nb
+    dev = dist.local_rank
+    jobs = serve_jobs(nb, args.serve_rate, args.serve_seconds, SERVE["seed"] + dist.rank)
+    clocks = ClockSampler(dev)
+    dist.barrier()
+    clocks.start()
+    served = run_serve_arm(nb, jobs, SERVE["dt"], dev)
+    clk = clocks.stop()
+    plain = run_plain_arm(nb, jobs, SERVE["dt"], dev) if not args.skip_plain else None
+    dist.barrier()
+    total = dist.sum(served["body_updates"])
+    span = dist.max(served["span_s"])
+    if dist.rank != 0:
+        return None
+    offered = sum(c.num_of_bodies * s for _, c, s in jobs) / args.serve_seconds
+    out = {
+        "metric": "served body-updates/s and job latency p50/p99, Poisson job stream",
+        "value": total / span,
+        "unit": "body-updates/s",
+        "n_gpus": dist.world,
+        "steps": None,
+        "warmup": 0,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded job stream; initial conditions generated by the server)",
+        "config": {"workload": SERVE["name"], "rate_jobs_per_s": args.serve_rate,
+                   "stream_seconds": args.serve_seconds, "jobs": len(jobs),
+                   "n_range": [SERVE["n_min"], SERVE["n_max"]], "steps_range": [SERVE["steps_min"], SERVE["steps_max"]],
+                   "thetas": list(SERVE["thetas"]), "eps": SERVE["eps"], "dt": SERVE["dt"],
+                   "direct_below": SERVE["direct_below"], "hbm_budget_bytes": SERVE["budget"],
+                   "snapshot_every": SERVE["snapshot_every"], "offered_body_updates_per_s": offered,
+                   "parallelism": f"replicas x{dist.world}"},
+        "served": served,
+        "plain": plain,
+        "served_over_plain": (served["value"] / plain["value"]) if plain else None,
+        "clocks": clk,
+    }
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -541,8 +691,12 @@ def main():
                     help="bodies per system (default the 4M workload; smaller sizes for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
     ap.add_argument("--skip-fp32", action="store_true", help="omit the plain-FP32 accumulation run")
-    ap.add_argument("--mode", choices=("step", "batch"), default="step",
-                    help="step: the 4M Barnes-Hut system; batch: 512 batched systems vs plain solves")
+    ap.add_argument("--mode", choices=("step", "batch", "serve"), default="step",
+                    help="step: the 4M Barnes-Hut system; batch: 512 batched systems vs plain solves; "
+                         "serve: a Poisson job stream through the job server vs plain solves")
+    ap.add_argument("--serve-rate", type=float, default=SERVE["rate"])
+    ap.add_argument("--serve-seconds", type=float, default=SERVE["seconds"])
+    ap.add_argument("--skip-plain", action="store_true", help="serve mode: omit the plain-solve arm")
     ap.add_argument("--systems", type=int, default=BATCH["systems"])
     ap.add_argument("--batch-steps", type=int, default=BATCH["steps"])
     ap.add_argument("--plain-steps", type=int, default=BATCH["plain_steps"])
@@ -555,6 +709,8 @@ def main():
             out = run_reference(args, dist)
         elif args.mode == "batch":
             out = run_batch(args, dist)
+        elif args.mode == "serve":
+            out = run_serve(args, dist)
         else:
             out = run_ours(args, dist)
         if dist.rank == 0 and out is not None:

@@ -311,6 +311,85 @@ nb_status nb_batch_autotune(nb_batch *b, const char *cache_path, int32_t *chosen
 nb_status nb_batch_info(nb_batch *b, int64_t out[8]);
 const char *nb_batch_last_error_message(const nb_batch *b);
 
+/* ---- job server: continuous batching of simulation jobs ----
+ * No counterpart in the reference (one interactive simulation per process);
+ * a serving layer over the batched step.
+ *
+ * Jobs (an nb_config, initial conditions, a step count and dt) are queued by
+ * nb_server_submit from any thread and admitted first come first served
+ * while a slot (max_jobs) and their device memory (bodies plus up to
+ * max(2N, 4096) tree cells, counted against hbm_budget_bytes) are free.  Their
+ * state stays resident in HBM while they run.  Every round of
+ * snapshot_every steps advances all running jobs together (one launch per
+ * stage over all of them, replayed as a CUDA graph); jobs admitted while a
+ * round runs join at the next round, and a job that finishes stops taking
+ * part at once.  Positions are returned every snapshot_every steps and the
+ * final positions and velocities at the end, through the callback (from a
+ * library thread) or, without one, by nb_server_result.  A job's result does
+ * not depend on what runs beside it (bit-identical alone and in a mix);
+ * tree jobs are also bit-identical to a standalone handle's nb_step, direct
+ * jobs equal to it within FP32 summation-order tolerance.  All jobs share
+ * numerical_method, precision and multipole (set in the server config; a
+ * job whose config differs is refused). */
+typedef struct nb_server nb_server;
+typedef struct nb_server_config {
+    int32_t device;
+    int32_t max_jobs;          /* jobs on the GPU at once */
+    int64_t hbm_budget_bytes;  /* device memory for job state */
+    int32_t snapshot_every;    /* steps between snapshots (0: none; rounds are then 10 steps) */
+    int32_t numerical_method;
+    int32_t precision;
+    int32_t multipole;
+    int32_t direct_variant;    /* direct-sum kernel shape (nb_batch_autotune's choice); -1: default */
+    int32_t reserved[7];
+} nb_server_config;
+enum { NB_JOB_QUEUED = 0, NB_JOB_RUNNING = 1, NB_JOB_DONE = 2, NB_JOB_FAILED = 3 };
+enum { NB_JOB_EVENT_SNAPSHOT = 0, NB_JOB_EVENT_DONE = 1, NB_JOB_EVENT_FAILED = 2 };
+/* event SNAPSHOT: value = steps done, pos3 (vel3 NULL); DONE: value = steps,
+ * pos3 and vel3; FAILED: value = the nb_status, no arrays.  The arrays are
+ * valid during the call only. */
+typedef void (*nb_job_fn)(void *user, int64_t job, int32_t event, int32_t value, const float *pos3,
+                          const float *vel3, int32_t n);
+void nb_server_config_default(nb_server_config *c);
+nb_status nb_server_create(const nb_server_config *c, nb_job_fn fn, void *user, nb_server **out);
+/* Copies the inputs.  pos3 == NULL: initial conditions are generated from
+ * cfg by nb_generate_ic on a server thread (vel3 and mass are then ignored);
+ * vel3 == NULL: zero velocities. */
+nb_status nb_server_submit(nb_server *s, const nb_config *cfg, int32_t steps, float dt, const float *pos3,
+                           const float *vel3, const float *mass, int64_t *job);
+typedef struct nb_job_info {
+    int32_t state;        /* NB_JOB_* */
+    int32_t status;       /* nb_status of a failed job */
+    int32_t steps;
+    int32_t n;
+    double t_submit;      /* seconds since nb_server_create */
+    double t_admit;
+    double t_done;
+    int64_t bytes;        /* device footprint */
+} nb_job_info;
+nb_status nb_server_job_info(nb_server *s, int64_t job, nb_job_info *out);
+/* Waits until the job (job < 0: every job submitted so far) has finished;
+ * NB_ERR_SPIN_TIMEOUT after timeout_s seconds (< 0: no limit). */
+nb_status nb_server_wait(nb_server *s, int64_t job, double timeout_s);
+/* Final state of a finished job when the server has no callback (copied
+ * once, then released); either array may be NULL. */
+nb_status nb_server_result(nb_server *s, int64_t job, float *pos3, float *vel3);
+typedef struct nb_server_stats {
+    int64_t submitted, completed, failed, queued, running;
+    int64_t rounds;
+    int64_t bytes_in_use, peak_bytes;
+    int32_t peak_jobs;
+    int32_t pad;
+    double body_updates;  /* sum of N * steps over completed jobs */
+    double first_submit_s, last_done_s;
+    double latency_p50_s, latency_p99_s, latency_max_s, latency_mean_s;
+} nb_server_stats;
+nb_status nb_server_get_stats(nb_server *s, nb_server_stats *out);
+/* Stops admitting, cancels queued and running jobs, waits for the GPU and
+ * frees everything. */
+nb_status nb_server_destroy(nb_server *s);
+const char *nb_server_last_error_message(const nb_server *s);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

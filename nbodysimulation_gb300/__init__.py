@@ -121,6 +121,15 @@ SIGNATURES = {
     "nb_batch_autotune": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
     "nb_batch_info": ([_P, _P], _I),
     "nb_batch_last_error_message": ([_P], ctypes.c_char_p),
+    "nb_server_config_default": ([_P], None),
+    "nb_server_create": ([_P, _P, _P, ctypes.POINTER(_P)], _I),
+    "nb_server_submit": ([_P, ctypes.POINTER(NbConfig), _I, _F, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)], _I),
+    "nb_server_job_info": ([_P, ctypes.c_int64, _P], _I),
+    "nb_server_wait": ([_P, ctypes.c_int64, _D], _I),
+    "nb_server_result": ([_P, ctypes.c_int64, _P, _P], _I),
+    "nb_server_get_stats": ([_P, _P], _I),
+    "nb_server_destroy": ([_P], _I),
+    "nb_server_last_error_message": ([_P], ctypes.c_char_p),
 }
 NOALLOC_MAX_BODIES = 65536
 
@@ -385,3 +394,124 @@ class Batch:
         keys = ("systems", "bodies", "tree_systems", "direct_systems", "launches_per_step", "direct_variant",
                 "launches", "interactions")
         return dict(zip(keys, (int(x) for x in out)))
+
+
+class NbServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("max_jobs", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
+                ("snapshot_every", ctypes.c_int32), ("numerical_method", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("multipole", ctypes.c_int32), ("direct_variant", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 7)]
+
+
+class NbJobInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("status", ctypes.c_int32), ("steps", ctypes.c_int32),
+                ("n", ctypes.c_int32), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double),
+                ("t_done", ctypes.c_double), ("bytes", ctypes.c_int64)]
+
+
+class NbServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("queued", ctypes.c_int64), ("running", ctypes.c_int64), ("rounds", ctypes.c_int64),
+                ("bytes_in_use", ctypes.c_int64), ("peak_bytes", ctypes.c_int64), ("peak_jobs", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("body_updates", ctypes.c_double), ("first_submit_s", ctypes.c_double),
+                ("last_done_s", ctypes.c_double), ("latency_p50_s", ctypes.c_double),
+                ("latency_p99_s", ctypes.c_double), ("latency_max_s", ctypes.c_double),
+                ("latency_mean_s", ctypes.c_double)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = range(4)
+JOB_EVENT_SNAPSHOT, JOB_EVENT_DONE, JOB_EVENT_FAILED = range(3)
+JOB_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                          ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_int32)
+
+
+def server_config(**kw) -> NbServerConfig:
+    c = NbServerConfig()
+    load().nb_server_config_default(ctypes.byref(c))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class Server:
+    """Job server (nb_server_*): continuous batching of simulation jobs.
+
+    on_event(job, event, value, pos, vel) is called from a library thread with
+    numpy copies of the arrays (None where absent); without it, finished
+    results are kept for result()."""
+
+    def __init__(self, cfg: NbServerConfig | None = None, on_event=None, copy_arrays=True, **kw):
+        self.L = load()
+        self.cfg = cfg if cfg is not None else server_config(**kw)
+        self._user_fn = on_event
+        self._fn = None
+        if on_event is not None:
+            def _cb(user, job, event, value, pos, vel, n):
+                p = v = None
+                if copy_arrays and pos:
+                    p = np.ctypeslib.as_array(pos, shape=(n, 3)).copy()
+                if copy_arrays and vel:
+                    v = np.ctypeslib.as_array(vel, shape=(n, 3)).copy()
+                on_event(int(job), int(event), int(value), p, v)
+            self._fn = JOB_FN(_cb)
+        h = ctypes.c_void_p()
+        fn_ptr = ctypes.cast(self._fn, ctypes.c_void_p) if self._fn is not None else None
+        st = self.L.nb_server_create(ctypes.byref(self.cfg), fn_ptr, None, ctypes.byref(h))
+        if st:
+            raise NbError(st, f"nb_server_create: {self.L.nb_status_string(st).decode()}")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.nb_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, what):
+        if st:
+            msg = self.L.nb_server_last_error_message(self.h).decode()
+            raise NbError(st, f"{what}: {msg or self.L.nb_status_string(st).decode()}")
+
+    def submit(self, cfg: NbConfig, steps, dt, pos=None, mass=None, vel=None):
+        jid = ctypes.c_int64(-1)
+        if pos is None:
+            st = self.L.nb_server_submit(self.h, ctypes.byref(cfg), steps, dt, None, None, None, ctypes.byref(jid))
+        else:
+            p = _f32(pos, (-1,))
+            m = _f32(mass, (-1,))
+            v = None if vel is None else _f32(vel, (-1,))
+            st = self.L.nb_server_submit(self.h, ctypes.byref(cfg), steps, dt, p.ctypes.data,
+                                         None if v is None else v.ctypes.data, m.ctypes.data, ctypes.byref(jid))
+        self._check(st, "nb_server_submit")
+        return jid.value
+
+    def info(self, job):
+        out = NbJobInfo()
+        self._check(self.L.nb_server_job_info(self.h, job, ctypes.byref(out)), "nb_server_job_info")
+        return {k: getattr(out, k) for k, _ in NbJobInfo._fields_}
+
+    def wait(self, job=-1, timeout=-1.0):
+        """Returns the job's status (0 when it finished normally)."""
+        return int(self.L.nb_server_wait(self.h, job, timeout))
+
+    def result(self, job, n):
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        self._check(self.L.nb_server_result(self.h, job, pos.ctypes.data, vel.ctypes.data), "nb_server_result")
+        return pos, vel
+
+    def stats(self):
+        out = NbServerStats()
+        self._check(self.L.nb_server_get_stats(self.h, ctypes.byref(out)), "nb_server_get_stats")
+        return {k: getattr(out, k) for k, _ in NbServerStats._fields_ if k != "pad"}

@@ -77,39 +77,12 @@ static void drop_graph(nb_batch *b) {
 static nb_status rebuild_tables(nb_batch *b) {
     const int ns = b->nsys;
     std::vector<int> pref(4 * (size_t)(ns + 1), 0);
-    int *chunk = &pref[0], *cell = &pref[ns + 1], *group = &pref[2 * (ns + 1)], *dblock = &pref[3 * (ns + 1)];
-    const int bb = batch_direct_block_bodies(b->variant);
-    int body = 0;
-    for (int k = 0; k < ns; ++k) {
-        SysDesc &d = b->h_sys[k];
-        const SysMem &m = b->mem[k];
-        d.body_begin = body;
-        d.chunk_begin = chunk[k];
-        d.cell_begin = cell[k];
-        d.group_begin = group[k];
-        d.dblock_begin = dblock[k];
-        const bool on = d.active != 0;
-        chunk[k + 1] = chunk[k] + (on && d.kind == kSysBH ? (m.n + kBatchChunk - 1) / kBatchChunk : 0);
-        cell[k + 1] = cell[k] + (on && d.kind == kSysBH ? m.cap + 1 : 0);
-        group[k + 1] = group[k] + (on && d.kind == kSysBH ? (m.n + 31) / 32 : 0);
-        dblock[k + 1] = dblock[k] + (on && d.kind == kSysDirect ? (m.n + bb - 1) / bb : 0);
-        body += m.n;
-    }
+    int totals[4];
+    batch_prefixes(b->h_sys.data(), ns, batch_direct_block_bodies(b->variant), pref.data(), totals);
     B_CUDA(b, cudaMemcpyAsync(b->d_sys, b->h_sys.data(), sizeof(SysDesc) * ns, cudaMemcpyHostToDevice, b->st));
     B_CUDA(b, cudaMemcpyAsync(b->d_pref, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, b->st));
     B_CUDA(b, cudaStreamSynchronize(b->st));
-    BatchTables &t = b->t;
-    t.sys = b->d_sys;
-    t.nsys = ns;
-    t.chunk_prefix = b->d_pref;
-    t.cell_prefix = b->d_pref + (ns + 1);
-    t.group_prefix = b->d_pref + 2 * (ns + 1);
-    t.dblock_prefix = b->d_pref + 3 * (ns + 1);
-    t.chunks = chunk[ns];
-    t.cells = cell[ns];
-    t.groups = group[ns];
-    t.dblocks = dblock[ns];
-    t.work = b->d_work;
+    b->t = batch_tables(b->d_sys, ns, b->d_pref, totals, b->d_work);
     drop_graph(b);
     return NB_OK;
 }
@@ -221,8 +194,10 @@ nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out) {
         cudaMalloc(&b->d_work, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&b->d_stage, sizeof(float) * 4 * (size_t)maxn) != cudaSuccess)
         return fail_all(NB_ERR_OUT_OF_MEMORY);
-    cudaMemset(b->d_ctrl, 0, sizeof(Ctrl) * nsys);
     memset(b->h_ctrl, 0, sizeof(Ctrl) * nsys);
+    for (int k = 0; k < nsys; ++k) b->h_ctrl[k].budget = -1;  // no step limit
+    if (cudaMemcpy(b->d_ctrl, b->h_ctrl, sizeof(Ctrl) * nsys, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail_all(NB_ERR_CUDA);
     b->h_sys.resize(nsys);
     for (int k = 0; k < nsys; ++k) {
         SysMem &m = b->mem[k];

@@ -22,7 +22,7 @@ __global__ void k_batch_reset(BatchTables t) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= t.nsys) return;
     const SysDesc &d = t.sys[k];
-    if (!d.active || d.kind != kSysBH) return;
+    if (!d.active || d.kind != kSysBH || !system_live(d.v.ctrl)) return;
     const DevSim &s = d.v;
     Ctrl *c = s.ctrl;
     c->bbox_key[0] = c->bbox_key[1] = c->bbox_key[2] = 0xFFFFFFFFu;
@@ -46,6 +46,7 @@ __global__ void k_batch_reset(BatchTables t) {
 __global__ void __launch_bounds__(256) k_batch_bbox(BatchTables t) {
     const int k = find_system(t.chunk_prefix, t.nsys, blockIdx.x);
     const SysDesc &d = t.sys[k];
+    if (!system_live(d.v.ctrl)) return;  // block-uniform
     const DevSim s = system_view(d);
     const int i0 = (blockIdx.x - d.chunk_begin) * kChunk;
     const int i1 = min(s.n, i0 + kChunk);
@@ -105,7 +106,7 @@ __global__ void __launch_bounds__(256) k_batch_build(BatchTables t) {
     const int k = find_system(t.chunk_prefix, t.nsys, blockIdx.x);
     const SysDesc &d = t.sys[k];
     const DevSim s = system_view(d);
-    if (read_status(s.ctrl)) return;
+    if (read_status(s.ctrl) || !system_live(s.ctrl)) return;
     const int i0 = (blockIdx.x - d.chunk_begin) * kChunk;
     const int i1 = min(s.n, i0 + kChunk);
     const int depth = d.p.tree_ref ? build_chunk<RefBox, true>(s, i0, i1) : build_chunk<GeoCube, false>(s, i0, i1);
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
         const int k = find_system(t.cell_prefix, t.nsys, x);
         const SysDesc &d = t.sys[k];
         const DevSim s = system_view(d);
-        if (read_status(s.ctrl)) continue;
+        if (read_status(s.ctrl) || !system_live(s.ctrl)) continue;
         const int node = s.n + (x - d.cell_begin);
         if (node < s.ctrl->bottom) continue;
         if (d.p.quadrupole) summarize_from<true>(s, node);
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(256) k_batch_sort(BatchTables t) {
         const int k = find_system(t.cell_prefix, t.nsys, x);
         const SysDesc &d = t.sys[k];
         const DevSim s = system_view(d);
-        if (read_status(s.ctrl)) continue;
+        if (read_status(s.ctrl) || !system_live(s.ctrl)) continue;
         const int node = s.n + s.cap - (x - d.cell_begin);
         if (node < s.ctrl->bottom) continue;
         sort_cell(s, node);
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
     const WarpStage ws{s_stack[w], s_bpm[w], s_cpm[w], s_cmeta[w], s_cqa[w]};
     float *dq = s_dq[w];
     int cur = -1;
-    bool skip = false;
+    int mode = 0;  // 0 walk, 1 keep the step-start state (failed step), 2 inert
     while (true) {
         int gg = 0;
         if (lane == 0) gg = atomicAdd(t.work, 1);
@@ -183,13 +184,16 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
             cur = k;
             int sk = 0;
             if (lane == 0) {
-                sk = read_status(s.ctrl);
-                if (!sk && s.ctrl->max_depth >= kMaxDepth) {
+                if (!system_live(s.ctrl)) {
+                    sk = 2;
+                } else if (read_status(s.ctrl)) {
+                    sk = 1;
+                } else if (s.ctrl->max_depth >= kMaxDepth) {
                     set_status(s.ctrl, kStDepth, s.ctrl->max_depth);
                     sk = 1;
                 }
             }
-            skip = __shfl_sync(0xffffffffu, sk, 0) != 0;
+            mode = __shfl_sync(0xffffffffu, sk, 0);
             __syncwarp();  // the previous system's thresholds are no longer read
             if (lane == 0) {
                 float box[6];
@@ -199,7 +203,8 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
             __syncwarp();
         }
         const int g = gg - d.group_begin;
-        if (skip) {  // keep the step-start state
+        if (mode == 2) continue;
+        if (mode == 1) {  // keep the step-start state
             const int i = g * 32 + lane;
             if (i < s.n) s.body_next[i] = s.body_cur[i];
             continue;
@@ -220,6 +225,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_direct(BatchTables t) {
     __shared__ __align__(8) uint64_t bar[2];
     const int k = find_system(t.dblock_prefix, t.nsys, blockIdx.x);
     const SysDesc &d = t.sys[k];
+    if (!system_live(d.v.ctrl)) return;  // block-uniform, before any barrier
     const DevSim s = system_view(d);
     StepParams p = d.p;
     p.kdk_primed = s.ctrl->kdk_primed;
@@ -295,15 +301,20 @@ __global__ void __launch_bounds__(kThreads) k_batch_direct(BatchTables t) {
 }
 
 // ---------------------------------------------------------------------------
-// flip: the next buffer becomes current; KDK systems are primed
+// flip: the next buffer becomes current; KDK systems are primed; one step
+// of the system's budget is used
 // ---------------------------------------------------------------------------
 __global__ void k_batch_flip(BatchTables t) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= t.nsys) return;
     const SysDesc &d = t.sys[k];
     if (!d.active) return;
-    d.v.ctrl->parity ^= 1;
-    if (d.p.method == 3) d.v.ctrl->kdk_primed = 1;
+    Ctrl *c = d.v.ctrl;
+    const int budget = c->budget;
+    if (budget == 0) return;
+    c->parity ^= 1;
+    if (d.p.method == 3) c->kdk_primed = 1;
+    if (budget > 0) c->budget = budget - 1;
 }
 
 // ---------------------------------------------------------------------------

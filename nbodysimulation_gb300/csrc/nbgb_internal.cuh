@@ -40,7 +40,8 @@ struct Ctrl {
     int work;              // dynamic work counter of the force pass
     int parity;            // batched systems: which body buffer is current
     int kdk_primed;        // batched systems: a KDK half-kick has happened
-    int pad0[3];
+    int budget;            // batched systems: steps left (< 0 unlimited, 0 inert)
+    int pad0[2];
     // cleared by the host once per nb_step call (everything from here on)
     int status;
     int status_info;
@@ -160,6 +161,9 @@ __device__ __forceinline__ int find_system(const int *prefix, int nsys, int x) {
     }
     return lo;
 }
+
+// A batched system with no steps left takes no part in any stage.
+__device__ __forceinline__ bool system_live(const Ctrl *c) { return ld_volatile(&c->budget) != 0; }
 
 __device__ __forceinline__ DevSim system_view(const SysDesc &d) {
     DevSim v = d.v;

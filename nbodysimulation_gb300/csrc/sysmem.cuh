@@ -119,4 +119,49 @@ inline SysDesc sysmem_desc(const SysMem &m, const nb_config &c, float dt) {
     return d;
 }
 
+// Where every system's work starts in the four batch-wide index spaces
+// (bbox/build chunks, cell slots, force warp groups, direct-sum blocks of
+// `direct_block` bodies).  Fills the *_begin fields of sys, the four prefix
+// tables (nsys + 1 entries each, back to back in pref) and their totals.
+inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, int totals[4]) {
+    int *chunk = pref, *cell = pref + (nsys + 1), *group = pref + 2 * (nsys + 1), *dblock = pref + 3 * (nsys + 1);
+    chunk[0] = cell[0] = group[0] = dblock[0] = 0;
+    int body = 0;
+    for (int k = 0; k < nsys; ++k) {
+        SysDesc &d = sys[k];
+        const int n = d.v.n;
+        d.body_begin = body;
+        d.chunk_begin = chunk[k];
+        d.cell_begin = cell[k];
+        d.group_begin = group[k];
+        d.dblock_begin = dblock[k];
+        const bool bh = d.active && d.kind == kSysBH, direct = d.active && d.kind == kSysDirect;
+        chunk[k + 1] = chunk[k] + (bh ? (n + kBatchChunk - 1) / kBatchChunk : 0);
+        cell[k + 1] = cell[k] + (bh ? d.v.cap + 1 : 0);
+        group[k + 1] = group[k] + (bh ? (n + 31) / 32 : 0);
+        dblock[k + 1] = dblock[k] + (direct ? (n + direct_block - 1) / direct_block : 0);
+        body += n;
+    }
+    totals[0] = chunk[nsys];
+    totals[1] = cell[nsys];
+    totals[2] = group[nsys];
+    totals[3] = dblock[nsys];
+}
+
+inline BatchTables batch_tables(const SysDesc *d_sys, int nsys, const int *d_pref, const int totals[4], int *work) {
+    BatchTables t{};
+    t.sys = d_sys;
+    t.nsys = nsys;
+    t.chunk_prefix = d_pref;
+    t.cell_prefix = d_pref + (nsys + 1);
+    t.group_prefix = d_pref + 2 * (nsys + 1);
+    t.dblock_prefix = d_pref + 3 * (nsys + 1);
+    t.chunks = totals[0];
+    t.cells = totals[1];
+    t.groups = totals[2];
+    t.dblocks = totals[3];
+    t.work = work;
+    return t;
+}
+
 }  // namespace nbgb
