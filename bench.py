@@ -306,7 +306,7 @@ def run_ours(args, dist: Dist):
     # 128 B and packed child quadrupoles 192 B read once
     alg_bytes = 84 * n + 352 * cells_used
     achieved = alg_bytes / (force_ms / 1e3) / 1e9
-    sm_mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    sm_mhz = (clk or {}).get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
     sm_count = device_sm_count(dev)
     inter_per_step = inter / args.steps
     flops_per_step = (FLOPS_PER_INTERACTION * inter + FLOPS_PER_QUADRUPOLE * cell_inter) / args.steps
@@ -352,7 +352,7 @@ def run_ours(args, dist: Dist):
                     "frac": flops_per_step / (force_ms / 1e3) / fp32_peak_ops,
                     "cells_opened_per_step": opened / args.steps,
                     "ops_model": "12 FP32 ops per interaction + 19 per cell quadrupole term",
-                    "peak_kind": "derived: 128 FP32 lanes x SMs x median sampled SM clock"},
+                    "peak_kind": "derived: 128 FP32 lanes x SMs x maximum SM clock"},
         "tree": {"cells_used": cells_used, "max_depth": int(info[3])},
         "clocks": clk,
     }
@@ -400,6 +400,80 @@ def run_reference(args, dist: Dist):
                    "wall_s": wall},
         "cpu_baseline": cb,
         "e2e": {"value": value, "unit": "body-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ---------------------------------------------------------------------------
+# direct sum: tiled all-pairs on N = 262,144 and the naive kernel on N = 4096
+# ---------------------------------------------------------------------------
+DIRECT = dict(n=262144, n_global=4096, eps=0.01, eps_global=0.05, dt=1e-3, G=1.0, steps=50)
+DIRECT_FP32_OPS = 12  # per pair: 3 FADD, 3 FFMA (d^2), 3 FMUL (r^3 m), 3 FFMA (accumulate); +1 MUFU rsqrt
+
+
+def direct_leg(nb, dev, n, tiled, eps, steps, warmup, sm_count, sm_mhz):
+    """Device time of `steps` direct-sum steps (Euler) and the FP32-pipe
+    roofline: interactions/s x 12 over 128 FP32 lanes x SMs x clock."""
+    cfg = nb.default_config(num_of_bodies=n, algo_config=nb.BRUTE_FORCE_LOCAL if tiled else nb.BRUTE_FORCE_GLOBAL,
+                            epsilon=eps, direct_epsilon=eps, gravitational_constant=DIRECT["G"],
+                            numerical_method=nb.EULER, device=dev,
+                            pos_config=nb.BALL_POS if tiled else nb.NORMAL_SIGMA_POS, pos_sigma=(1.0, 1.0, 1.0),
+                            starting_volume_radius=1.0, vel_config=nb.CIRCULAR_Z_VEL if tiled else nb.FUNC_ZERO_VEL,
+                            mass_config=nb.MASS_EQUAL, seed=0)
+    pos, vel, mass = nb.generate_ic(cfg)
+    with nb.Simulation(cfg) as s:
+        s.set_state(pos, mass, vel)
+        s.step(DIRECT["dt"], warmup)
+        ms = s.time_steps(DIRECT["dt"], steps)
+        rng = np.random.default_rng(99)
+        sample = rng.choice(n, min(n, PROBE_SAMPLES), replace=False).astype(np.int32)
+        err_max, err_rms, _ = s.force_error(sample)
+    inter = float(n) * n * steps
+    ips = inter / (ms / 1e3)
+    peak_ips = FP32_LANES_PER_SM * sm_count * sm_mhz * 1e6 / DIRECT_FP32_OPS
+    return {"kernel": "k_direct_tiled" if tiled else "k_direct_global", "n_bodies": n, "eps": eps,
+            "steps": steps, "ms_per_step": ms / steps, "body_updates_per_s": n * steps / (ms / 1e3),
+            "interactions_per_s": ips, "fp32_gops": ips * DIRECT_FP32_OPS / 1e9,
+            "roofline": {"bound": "fp32", "achieved": ips * DIRECT_FP32_OPS / 1e12,
+                         "peak": FP32_LANES_PER_SM * sm_count * sm_mhz * 1e6 / 1e12, "unit": "TFLOP/s (FP32 ops)",
+                         "frac": ips / peak_ips,
+                         "peak_kind": "derived: 128 FP32 lanes x SMs x maximum SM clock"},
+            "gflops_20_per_pair": ips * 20 / 1e9,
+            "accuracy": {"rms_rel_err": err_rms, "max_rel_err": err_max, "samples": int(len(sample)),
+                         "oracle": "FP64 direct sum on the GPU"}}
+
+
+def run_direct(args, dist: Dist):
+    from nbodysimulation_gb300 import build as nbbuild
+    if dist.local_rank == 0:
+        nbbuild.build()
+    dist.barrier()
+    import nbodysimulation_gb300 as nb
+    dev = dist.local_rank
+    sm_count = device_sm_count(dev)
+    peaks, _ = measured_peaks()
+    steps = max(args.steps, DIRECT["steps"])
+    max_mhz = peaks.get("sm_max_mhz", 2070.0)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    tiled = direct_leg(nb, dev, DIRECT["n"], True, DIRECT["eps"], steps, args.warmup, sm_count, max_mhz)
+    clk = clocks.stop()
+    glob = direct_leg(nb, dev, DIRECT["n_global"], False, DIRECT["eps_global"], 20, args.warmup, sm_count, max_mhz)
+    ms = dist.max(tiled["ms_per_step"] * steps)
+    if dist.rank != 0:
+        return None
+    return {
+        "metric": "direct-sum interactions/s, tiled N=262144 (FP32 roofline fraction)",
+        "value": dist.world * float(DIRECT["n"]) ** 2 * steps / (ms / 1e3),
+        "unit": "interactions/s",
+        "n_gpus": dist.world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded unit ball with circular z velocities, masses 1/N)",
+        "config": {"workload": "direct_tiled_n262144", "n_bodies": DIRECT["n"], "eps": DIRECT["eps"],
+                   "dt": DIRECT["dt"], "G": DIRECT["G"], "integrator": "euler",
+                   "l2": "inputs (4 MiB) fit in L2: the sum is compute-bound, no flush needed",
+                   "parallelism": f"replicas x{dist.world}"},
+        "tiled": tiled, "global_n4096": glob, "clocks": clk,
     }
 
 
@@ -691,7 +765,7 @@ def main():
                     help="bodies per system (default the 4M workload; smaller sizes for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
     ap.add_argument("--skip-fp32", action="store_true", help="omit the plain-FP32 accumulation run")
-    ap.add_argument("--mode", choices=("step", "batch", "serve"), default="step",
+    ap.add_argument("--mode", choices=("step", "batch", "serve", "direct"), default="step",
                     help="step: the 4M Barnes-Hut system; batch: 512 batched systems vs plain solves; "
                          "serve: a Poisson job stream through the job server vs plain solves")
     ap.add_argument("--serve-rate", type=float, default=SERVE["rate"])
@@ -711,6 +785,8 @@ def main():
             out = run_batch(args, dist)
         elif args.mode == "serve":
             out = run_serve(args, dist)
+        elif args.mode == "direct":
+            out = run_direct(args, dist)
         else:
             out = run_ours(args, dist)
         if dist.rank == 0 and out is not None:

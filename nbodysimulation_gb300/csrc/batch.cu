@@ -34,7 +34,7 @@ struct nb_batch {
     Ctrl *h_ctrl = nullptr;     // pinned mirror
     std::vector<SysDesc> h_sys;
     SysDesc *d_sys = nullptr;
-    int *d_pref = nullptr;      // 4 prefix tables of nsys + 1
+    int *d_pref = nullptr;      // 5 prefix tables of nsys + 1 (the last written on the device)
     int *d_work = nullptr;
     float *d_stage = nullptr;   // 4 * max N floats of transfer staging
     BatchTables t{};
@@ -190,7 +190,7 @@ nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out) {
     if (cudaMalloc(&b->d_ctrl, sizeof(Ctrl) * nsys) != cudaSuccess ||
         cudaMallocHost(&b->h_ctrl, sizeof(Ctrl) * nsys) != cudaSuccess ||
         cudaMalloc(&b->d_sys, sizeof(SysDesc) * nsys) != cudaSuccess ||
-        cudaMalloc(&b->d_pref, sizeof(int) * 4 * (size_t)(nsys + 1)) != cudaSuccess ||
+        cudaMalloc(&b->d_pref, sizeof(int) * 5 * (size_t)(nsys + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_work, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&b->d_stage, sizeof(float) * 4 * (size_t)maxn) != cudaSuccess)
         return fail_all(NB_ERR_OUT_OF_MEMORY);

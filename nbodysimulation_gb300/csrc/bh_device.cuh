@@ -300,13 +300,15 @@ __device__ __forceinline__ bool sort_cell(const DevSim &s, int k) {
     const int c = k - n;
     int st = ld_volatile(&s.start[c]);
     long long spins = 0;
+    unsigned pause = 32;  // back off: many waiting threads must not flood L2 with polls
     while (st < 0) {
         if (++spins > kSpinCap) {
             set_status(ctrl, kStSpinTimeout, k);
             return false;
         }
         if ((spins & 1023) == 0 && read_status(ctrl)) return false;
-        __nanosleep(32);
+        __nanosleep(pause);
+        if (pause < 1024) pause <<= 1;
         st = ld_volatile(&s.start[c]);
     }
     const int4 a0 = *reinterpret_cast<const int4 *>(&s.wchild[c * 8]);

@@ -166,7 +166,7 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
             const float4 q = bpm[k];
             const float dx = q.x - P.x, dy = q.y - P.y, dz = q.z - P.z;
             const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-            const float r = rsqrtf(d2);
+            const float r = rsqrt_fast(d2);
             float F = q.w * (r * (r * r));
             if constexpr (kEpsZero) F = d2 > 0.0f ? F : 0.0f;
             sx = fmaf(dx, F, sx);
@@ -181,7 +181,7 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
             const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
             if (__all_sync(0xffffffffu, d2 >= mt.z)) {
                 ++n_cell;
-                const float r = rsqrtf(d2);
+                const float r = rsqrt_fast(d2);
                 const float r2 = r * r;
                 const float r3 = r * r2;
                 float F = q.w * r3;

@@ -5,8 +5,9 @@
 // finds its system with a binary search in the stage's prefix table.
 // Barnes-Hut systems run the same per-item code as the single-system
 // kernels (bh_device.cuh, force_device.cuh); small systems take the
-// TMA-tiled direct sum.  A step is: reset, bbox, build, summarize, sort,
-// force, direct, flip -- captured once into a CUDA graph by the host.
+// TMA-tiled direct sum.  A step is: reset, bbox, build, used-cell scan,
+// summarize, sort, force, direct, flip -- captured once into a CUDA graph by
+// the host.
 #include "bh_device.cuh"
 #include "force_device.cuh"
 #include "tma.cuh"
@@ -117,38 +118,85 @@ __global__ void __launch_bounds__(256) k_batch_build(BatchTables t) {
 }
 
 // ---------------------------------------------------------------------------
-// summarize: one cell slot per thread over all systems' slot ranges
+// used cells: after the build, every tree's allocated cells [bottom, root]
+// are laid end to end (one exclusive scan over the systems, one block), so
+// summarize and sort visit only cells that exist.  A tree whose step failed,
+// or that has no steps left, contributes none.
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) k_batch_used(BatchTables t) {
+    __shared__ int warp_sum[kScanThreads / 32];
+    __shared__ int carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < t.nsys; base += kScanThreads) {
+        const int k = base + threadIdx.x;
+        int used = 0;
+        if (k < t.nsys) {
+            const SysDesc &d = t.sys[k];
+            const Ctrl *c = d.v.ctrl;
+            if (d.active && d.kind == kSysBH && system_live(c) && !read_status(c))
+                used = d.v.n + d.v.cap - c->bottom + 1;
+        }
+        int incl = used;  // inclusive scan: warps, then warp totals
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_sum[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            int v = warp_sum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            warp_sum[lane] = v;  // inclusive over warps
+        }
+        __syncthreads();
+        const int before = carry + (w > 0 ? warp_sum[w - 1] : 0) + incl - used;
+        if (k < t.nsys) t.used_prefix[k] = before;
+        __syncthreads();
+        if (threadIdx.x == kScanThreads - 1) carry = before + used;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) t.used_prefix[t.nsys] = carry;
+}
+
+// ---------------------------------------------------------------------------
+// summarize: one allocated cell per thread over all trees
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
+    const int total = t.used_prefix[t.nsys];
     const int stride = gridDim.x * blockDim.x;
-    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < t.cells; x += stride) {
-        const int k = find_system(t.cell_prefix, t.nsys, x);
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
+        const int k = find_system(t.used_prefix, t.nsys, x);
         const SysDesc &d = t.sys[k];
         const DevSim s = system_view(d);
-        if (read_status(s.ctrl) || !system_live(s.ctrl)) continue;
-        const int node = s.n + (x - d.cell_begin);
-        if (node < s.ctrl->bottom) continue;
+        const int node = s.ctrl->bottom + (x - t.used_prefix[k]);
         if (d.p.quadrupole) summarize_from<true>(s, node);
         else summarize_from<false>(s, node);
     }
 }
 
 // ---------------------------------------------------------------------------
-// sort: inside every system the slots are visited in descending node order
-// (a parent before its children); the grid is no larger than what is
+// sort: inside every tree the cells are visited from the root downward (a
+// parent before its children); the grid is no larger than what is
 // co-resident, so every bounded wait in sort_cell is for a cell another
 // running thread handles in an earlier or the same round.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_batch_sort(BatchTables t) {
+    const int total = t.used_prefix[t.nsys];
     const int stride = gridDim.x * blockDim.x;
-    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < t.cells; x += stride) {
-        const int k = find_system(t.cell_prefix, t.nsys, x);
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
+        const int k = find_system(t.used_prefix, t.nsys, x);
         const SysDesc &d = t.sys[k];
         const DevSim s = system_view(d);
-        if (read_status(s.ctrl) || !system_live(s.ctrl)) continue;
-        const int node = s.n + s.cap - (x - d.cell_begin);
-        if (node < s.ctrl->bottom) continue;
-        sort_cell(s, node);
+        if (read_status(s.ctrl)) continue;
+        sort_cell(s, s.n + s.cap - (x - t.used_prefix[k]));
     }
 }
 
@@ -269,7 +317,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_direct(BatchTables t) {
             for (int r = 0; r < kI; ++r) {
                 const float dx = q.x - me[r].x, dy = q.y - me[r].y, dz = q.z - me[r].z;
                 const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-                const float rr = rsqrtf(d2);
+                const float rr = rsqrt_fast(d2);
                 const float F = (q.w * rr) * (rr * rr);
                 ax[r] = fmaf(dx, F, ax[r]);
                 ay[r] = fmaf(dy, F, ay[r]);
@@ -333,7 +381,8 @@ struct DirectVariant {
     int ki, threads, tile;
 };
 static const DirectVariant kDirectVariants[] = {{1, 128, 128}, {1, 128, 256}, {1, 256, 256}, {2, 128, 128},
-                                                {2, 128, 256}, {2, 256, 256}, {4, 128, 256}, {4, 256, 256}};
+                                                {2, 128, 256}, {2, 256, 256}, {4, 128, 256}, {4, 256, 256},
+                                                {1, 64, 256},  {2, 64, 256},  {4, 64, 256}};
 constexpr int kNumDirectVariants = sizeof(kDirectVariants) / sizeof(kDirectVariants[0]);
 
 int batch_direct_variants() { return kNumDirectVariants; }
@@ -352,7 +401,10 @@ static cudaError_t launch_direct_variant(const BatchTables &t, int variant, cuda
     case 4: k_batch_direct<2, 128, 256><<<b, 128, 0, st>>>(t); break;
     case 5: k_batch_direct<2, 256, 256><<<b, 256, 0, st>>>(t); break;
     case 6: k_batch_direct<4, 128, 256><<<b, 128, 0, st>>>(t); break;
-    default: k_batch_direct<4, 256, 256><<<b, 256, 0, st>>>(t); break;
+    case 7: k_batch_direct<4, 256, 256><<<b, 256, 0, st>>>(t); break;
+    case 8: k_batch_direct<1, 64, 256><<<b, 64, 0, st>>>(t); break;
+    case 9: k_batch_direct<2, 64, 256><<<b, 64, 0, st>>>(t); break;
+    default: k_batch_direct<4, 64, 256><<<b, 64, 0, st>>>(t); break;
     }
     return cudaGetLastError();
 }
@@ -386,6 +438,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
         k_batch_reset<<<sb, 128, 0, st>>>(t);
         k_batch_bbox<<<t.chunks, 256, 0, st>>>(t);
         k_batch_build<<<t.chunks, 256, 0, st>>>(t);
+        k_batch_used<<<1, kScanThreads, 0, st>>>(t);
         int sblocks = sm_count * 8;
         const int need = (t.cells + 255) / 256;
         if (sblocks > need) sblocks = need;
@@ -401,7 +454,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
         default: e = launch_batch_force_m<0>(t, comp, quad, sm_count, st); break;
         }
         if (e != cudaSuccess) return e;
-        nl += 6;
+        nl += 7;
     }
     if (t.dblocks > 0) {
         if ((e = launch_direct_variant(t, direct_variant, st)) != cudaSuccess) return e;

@@ -14,8 +14,9 @@
 
 namespace nbgb {
 
-constexpr int kTile = 256;        // bodies per staged tile (4 KiB)
-constexpr int kDirectThreads = 256;
+constexpr int kTile = 256;          // bodies per staged tile (4 KiB)
+constexpr int kDirectThreads = 256;  // collision kernel
+constexpr int kTiledThreads = 64;    // tiled direct sum: small blocks, many per SM, even load
 
 // ---- pair interactions ----
 template <bool kQuirk, bool kEpsZero>
@@ -23,7 +24,7 @@ __device__ __forceinline__ void pair(const float4 me, const float4 q, float eps2
     const float dx = q.x - me.x, dy = q.y - me.y, dz = q.z - me.z;
     if constexpr (!kQuirk) {
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-        const float r = rsqrtf(d2);
+        const float r = rsqrt_fast(d2);
         float F = (q.w * r) * (r * r);
         if constexpr (kEpsZero) F = d2 > 0.0f ? F : 0.0f;
         ax = fmaf(dx, F, ax);
@@ -106,25 +107,35 @@ __global__ void __launch_bounds__(256) k_direct_global(DevSim s, StepParams p, f
 // ---------------------------------------------------------------------------
 // direct_tiled (update_local, brute_force_update.cl:128-228): TMA-staged
 // j-tiles.  The reference's tile loop reloads tile 0 and skips the wrong body
-// (:167-184); here every j is visited once.  gridDim.y > 1 splits the j range
-// and accumulates partial accelerations into `part` (float atomics).
+// (:167-184); here every j is visited once.
+//
+// A block is kG groups of 64 threads that share the same 64*kI targets and
+// split the j range between them: each stage brings kG consecutive tiles,
+// group g takes the g-th, and at the end the groups' partial sums are added
+// in group order (deterministic).  More warps per target set hide the MUFU
+// and shared-memory latencies without more shared-memory loads per pair.
+// gridDim.y > 1 splits the j range over blocks as well and accumulates the
+// partial accelerations into `part` (float atomics).
 // ---------------------------------------------------------------------------
-template <int kI, int kMethod, bool kQuirk, bool kEpsZero>
-__global__ void __launch_bounds__(kDirectThreads) k_direct_tiled(DevSim s, StepParams p, float eps, float4 *part) {
-    __shared__ __align__(128) float4 tile[2][kTile];
+template <int kI, int kG, int kMethod, bool kQuirk, bool kEpsZero>
+__global__ void __launch_bounds__(kTiledThreads *kG) k_direct_tiled(DevSim s, StepParams p, float eps, float4 *part) {
+    __shared__ __align__(128) float4 tile[2][kG][kTile];
     __shared__ __align__(8) uint64_t bar[2];
+    __shared__ float red[kG > 1 ? kG - 1 : 1][3 * kI][kTiledThreads];
     const int n = s.n;
+    const int grp = threadIdx.x / kTiledThreads, gl = threadIdx.x % kTiledThreads;
     const int ntiles = (n + kTile - 1) / kTile;
     const int per_split = (ntiles + gridDim.y - 1) / gridDim.y;
     const int t0 = blockIdx.y * per_split;
     const int t1 = min(ntiles, t0 + per_split);
+    const int nst = (t1 - t0 + kG - 1) / kG;  // stages of kG tiles
     const float eps2 = eps * eps;
     int idx[kI];
     float4 me[kI];
     float ax[kI], ay[kI], az[kI];
 #pragma unroll
     for (int r = 0; r < kI; ++r) {
-        idx[r] = blockIdx.x * (kDirectThreads * kI) + r * kDirectThreads + threadIdx.x;
+        idx[r] = blockIdx.x * (kTiledThreads * kI) + r * kTiledThreads + gl;
         me[r] = idx[r] < n ? s.body_cur[idx[r]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         ax[r] = ay[r] = az[r] = 0.0f;
     }
@@ -134,21 +145,31 @@ __global__ void __launch_bounds__(kDirectThreads) k_direct_tiled(DevSim s, StepP
         mbar_fence_init();
     }
     __syncthreads();
-    auto issue = [&](int t, int stage) {
-        const int cnt = min(kTile, n - t * kTile);
-        const uint32_t bytes = (uint32_t)cnt * 16u;
-        mbar_expect_tx(&bar[stage], bytes);
-        bulk_g2s(&tile[stage][0], s.body_cur + (size_t)t * kTile, bytes, &bar[stage]);
+    auto issue = [&](int st, int stage) {
+        uint32_t total = 0;
+#pragma unroll
+        for (int g = 0; g < kG; ++g) {
+            const int t = t0 + st * kG + g;
+            if (t < t1) total += (uint32_t)min(kTile, n - t * kTile) * 16u;
+        }
+        mbar_expect_tx(&bar[stage], total);
+#pragma unroll
+        for (int g = 0; g < kG; ++g) {
+            const int t = t0 + st * kG + g;
+            if (t < t1)
+                bulk_g2s(&tile[stage][g][0], s.body_cur + (size_t)t * kTile,
+                         (uint32_t)min(kTile, n - t * kTile) * 16u, &bar[stage]);
+        }
     };
-    if (threadIdx.x == 0 && t0 < t1) issue(t0, 0);
+    if (threadIdx.x == 0 && nst > 0) issue(0, 0);
     bool ok = true;
-    for (int t = t0; t < t1; ++t) {
-        const int it = t - t0;
-        const int stage = it & 1;
-        if (threadIdx.x == 0 && t + 1 < t1) issue(t + 1, stage ^ 1);
-        if (!mbar_wait_bounded(&bar[stage], (uint32_t)((it >> 1) & 1), s.ctrl)) ok = false;
-        const int cnt = min(kTile, n - t * kTile);
-        const float4 *tl = tile[stage];
+    for (int st = 0; st < nst; ++st) {
+        const int stage = st & 1;
+        if (threadIdx.x == 0 && st + 1 < nst) issue(st + 1, stage ^ 1);
+        if (!mbar_wait_bounded(&bar[stage], (uint32_t)((st >> 1) & 1), s.ctrl)) ok = false;
+        const int t = t0 + st * kG + grp;
+        const int cnt = t < t1 ? min(kTile, n - t * kTile) : 0;
+        const float4 *tl = tile[stage][grp];
         if (cnt == kTile) {
 #pragma unroll 4
             for (int j = 0; j < kTile; ++j) {
@@ -164,14 +185,35 @@ __global__ void __launch_bounds__(kDirectThreads) k_direct_tiled(DevSim s, StepP
             }
         }
         if (!__syncthreads_and(ok)) {
-            // drain the copy already issued for the next tile before leaving
-            if (threadIdx.x == 0 && t + 1 < t1)
-                mbar_wait_bounded(&bar[stage ^ 1], (uint32_t)(((it + 1) >> 1) & 1), s.ctrl);
+            // drain the copies already issued for the next stage before leaving
+            if (threadIdx.x == 0 && st + 1 < nst)
+                mbar_wait_bounded(&bar[stage ^ 1], (uint32_t)(((st + 1) >> 1) & 1), s.ctrl);
             ok = false;
             break;
         }
     }
     if (!ok) return;
+    if constexpr (kG > 1) {
+        if (grp > 0) {
+#pragma unroll
+            for (int r = 0; r < kI; ++r) {
+                red[grp - 1][3 * r][gl] = ax[r];
+                red[grp - 1][3 * r + 1][gl] = ay[r];
+                red[grp - 1][3 * r + 2][gl] = az[r];
+            }
+        }
+        __syncthreads();
+        if (grp > 0) return;
+#pragma unroll
+        for (int g = 1; g < kG; ++g) {
+#pragma unroll
+            for (int r = 0; r < kI; ++r) {
+                ax[r] += red[g - 1][3 * r][gl];
+                ay[r] += red[g - 1][3 * r + 1][gl];
+                az[r] += red[g - 1][3 * r + 2][gl];
+            }
+        }
+    }
 #pragma unroll
     for (int r = 0; r < kI; ++r) {
         if (idx[r] >= n) continue;
@@ -315,30 +357,33 @@ static cudaError_t launch_direct_t(const DevSim &s, const StepParams &p, float e
         k_direct_global<kMethod, kQuirk, kEpsZero><<<(n + 255) / 256, 256, 0, st>>>(s, p, eps);
         return cudaGetLastError();
     }
-    // pick bodies per thread so the i-blocks fill the GPU, split j otherwise
-    const int want = sm_count * 2;
-    int bx4 = (n + kDirectThreads * 4 - 1) / (kDirectThreads * 4);
-    int bx2 = (n + kDirectThreads * 2 - 1) / (kDirectThreads * 2);
-    int bx1 = (n + kDirectThreads - 1) / kDirectThreads;
+    // bodies per thread: the most that still gives at least six blocks per
+    // SM (every block does the same work, so many small blocks keep the SMs
+    // evenly loaded), two j-groups per block; below that, split the j range
+    // over gridDim.y
+    const int want = sm_count * 6;
+    const int bx4 = (n + kTiledThreads * 4 - 1) / (kTiledThreads * 4);
+    const int bx2 = (n + kTiledThreads * 2 - 1) / (kTiledThreads * 2);
+    const int bx1 = (n + kTiledThreads - 1) / kTiledThreads;
     const int ntiles = (n + kTile - 1) / kTile;
     if (bx4 >= want) {
-        k_direct_tiled<4, kMethod, kQuirk, kEpsZero><<<dim3(bx4, 1), kDirectThreads, 0, st>>>(s, p, eps, part);
+        k_direct_tiled<4, 2, kMethod, kQuirk, kEpsZero><<<dim3(bx4, 1), 2 * kTiledThreads, 0, st>>>(s, p, eps, part);
         return cudaGetLastError();
     }
     if (bx2 >= want) {
-        k_direct_tiled<2, kMethod, kQuirk, kEpsZero><<<dim3(bx2, 1), kDirectThreads, 0, st>>>(s, p, eps, part);
+        k_direct_tiled<2, 2, kMethod, kQuirk, kEpsZero><<<dim3(bx2, 1), 2 * kTiledThreads, 0, st>>>(s, p, eps, part);
         return cudaGetLastError();
     }
     int split = (want + bx1 - 1) / bx1;
     if (split > ntiles) split = ntiles;
     if (split < 1) split = 1;
     if (split == 1) {
-        k_direct_tiled<1, kMethod, kQuirk, kEpsZero><<<dim3(bx1, 1), kDirectThreads, 0, st>>>(s, p, eps, part);
+        k_direct_tiled<1, 1, kMethod, kQuirk, kEpsZero><<<dim3(bx1, 1), kTiledThreads, 0, st>>>(s, p, eps, part);
         return cudaGetLastError();
     }
     cudaError_t e = cudaMemsetAsync(part, 0, sizeof(float4) * (size_t)n, st);
     if (e != cudaSuccess) return e;
-    k_direct_tiled<1, kMethod, kQuirk, kEpsZero><<<dim3(bx1, split), kDirectThreads, 0, st>>>(s, p, eps, part);
+    k_direct_tiled<1, 1, kMethod, kQuirk, kEpsZero><<<dim3(bx1, split), kTiledThreads, 0, st>>>(s, p, eps, part);
     k_integrate_partial<kMethod><<<(n + 255) / 256, 256, 0, st>>>(s, p, part);
     return cudaGetLastError();
 }

@@ -94,6 +94,17 @@ __device__ __forceinline__ float key2f(unsigned k) {
     return __uint_as_float(b);
 }
 
+// Reciprocal square root on the MUFU unit with subnormal inputs flushed
+// (PTX rsqrt.approx.ftz.f32).  The pair sums only take it of d^2 + eps^2,
+// which is normal or zero; without the flush the compiler wraps the MUFU
+// instruction in a rescaling for subnormal inputs that costs issue slots in
+// the innermost loops.
+__device__ __forceinline__ float rsqrt_fast(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ void set_status(Ctrl *c, int code, int info) {
     if (atomicCAS(&c->status, 0, code) == 0) c->status_info = info;
 }
@@ -149,7 +160,8 @@ struct BatchTables {
     int nsys;
     const int *chunk_prefix, *cell_prefix, *group_prefix, *dblock_prefix;
     int chunks, cells, groups, dblocks;
-    int *work;  // batch-wide force work counter
+    int *work;         // batch-wide force work counter
+    int *used_prefix;  // nsys + 1: prefix over the cells each tree allocated this step (device-written)
 };
 
 __device__ __forceinline__ int find_system(const int *prefix, int nsys, int x) {

@@ -521,7 +521,7 @@ nb_status nb_server_create(const nb_server_config *c, nb_job_fn fn, void *user, 
               cudaMalloc(&s->d_work, sizeof(int)) == cudaSuccess;
     for (int b = 0; b < 2 && ok; ++b) {
         ok = cudaMalloc(&s->d_sys[b], sizeof(SysDesc) * ns) == cudaSuccess &&
-             cudaMalloc(&s->d_pref[b], sizeof(int) * 4 * (ns + 1)) == cudaSuccess &&
+             cudaMalloc(&s->d_pref[b], sizeof(int) * 5 * (ns + 1)) == cudaSuccess &&
              cudaMallocHost(&s->h_sys[b], sizeof(SysDesc) * ns) == cudaSuccess &&
              cudaMallocHost(&s->h_pref[b], sizeof(int) * 4 * (ns + 1)) == cudaSuccess &&
              cudaEventCreateWithFlags(&s->round_ev[b], cudaEventDisableTiming) == cudaSuccess;

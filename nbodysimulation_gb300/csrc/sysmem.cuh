@@ -148,7 +148,9 @@ inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, 
     totals[3] = dblock[nsys];
 }
 
-inline BatchTables batch_tables(const SysDesc *d_sys, int nsys, const int *d_pref, const int totals[4], int *work) {
+// d_pref holds the four prefix tables of batch_prefixes followed by room for
+// the device-written table of used cells: 5 * (nsys + 1) ints.
+inline BatchTables batch_tables(const SysDesc *d_sys, int nsys, int *d_pref, const int totals[4], int *work) {
     BatchTables t{};
     t.sys = d_sys;
     t.nsys = nsys;
@@ -161,6 +163,7 @@ inline BatchTables batch_tables(const SysDesc *d_sys, int nsys, const int *d_pre
     t.groups = totals[2];
     t.dblocks = totals[3];
     t.work = work;
+    t.used_prefix = d_pref + 4 * (nsys + 1);
     return t;
 }
 

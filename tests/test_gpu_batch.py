@@ -62,7 +62,7 @@ def test_mixed_batch_matches_standalone(gpu, method, precision, quad):
         info = b.info()
         assert info["systems"] == len(SIZES)
         assert info["tree_systems"] == sum(1 for _, bh in SIZES if bh)
-        assert info["launches_per_step"] == 8  # reset bbox build summarize sort force direct flip
+        assert info["launches_per_step"] == 9  # reset bbox build used summarize sort force direct flip
         for k, ((n, bh), (p, m, v)) in enumerate(zip(SIZES, states)):
             got = b.get_state(k)
             ref = standalone(nb, cfgs[k], p, m, v, dt, steps)
@@ -136,7 +136,7 @@ def test_autotune_cache_and_unchanged_state(gpu, tmp_path):
             return chosen, b.info()["direct_variant"], [b.get_state(k) for k in range(len(sizes))]
 
     chosen, variant, tuned = run(True)
-    assert 0 <= chosen < 8 and variant == chosen
+    assert 0 <= chosen < 11 and variant == chosen
     table = json.loads(cache.read_text())
     assert list(table.values()) == [chosen]
     chosen2, _, again = run(True)  # read back from the cache
