@@ -15,6 +15,17 @@ nb_set_state from pinned host arrays, nb_step, nb_get_state into pinned host
 arrays.  The accuracy gate (RMS relative force error vs an FP64 direct sum
 on 8192 sample bodies <= 1e-3) is evaluated after the timed region.
 
+The same line carries three more measurements, each with its own timed
+region (and each available alone through --mode):
+  direct   the TMA-tiled direct sum on N = 262,144 (interactions/s against
+           the FP32-pipe roofline) and the naive kernel on N = 4096;
+  batched  512 systems, N log-uniform in [1024, 262144], one CUDA graph per
+           step, against a loop of plain solves (one handle per system);
+  serving  a seeded Poisson job stream (200 jobs/s; N log-uniform in
+           [1024, 2^20], 10-500 steps) through the job server, p50/p99 job
+           latency and served body-updates/s, against plain solves one job
+           at a time.
+
 Under torchrun (--gpus N > 1) every rank advances its own independent
 system on its own GPU (replicas; no exchange); rank 0 prints the aggregate.
 --impl reference times the CPU restatement of the reference's kernels
@@ -42,7 +53,7 @@ WORKLOAD = dict(name="bh_plummer_n4m_theta0.5", n=4194304, sigma=(1.0, 1.0, 0.2)
 PROBE_SAMPLES = 8192
 FP32_LANES_PER_SM = 128
 FLOPS_PER_INTERACTION = 12  # FP32 ops per monopole interaction (3 sub, 3 fma, 3 mul, 3 fma)
-FORCE_DRAM_BYTES_PER_BODY = (386.390528e6 + 75.163648e6) / 1048576  # dram read + write, k_force, N = 1M
+FORCE_DRAM_BYTES_PER_BODY = (387.995392e6 + 75.690752e6) / 1048576  # dram read + write, k_force, N = 1M
 FLOPS_PER_QUADRUPOLE = 19   # extra FP32 ops per cell quadrupole term (Q.d 9, d.Q.d 3, r^5 r^7 2, 2.5*sq 1, 4 fma)
 
 
@@ -610,7 +621,7 @@ def run_batch(args, dist: Dist):
 # ---------------------------------------------------------------------------
 SERVE = dict(name="serve_poisson200_n1k_1m", rate=200.0, seconds=2.0, n_min=1024, n_max=1048576, steps_min=10,
              steps_max=500, thetas=(0.5, 0.7), eps=0.01, dt=1e-3, G=1.0, direct_below=8192, budget=120e9,
-             snapshot_every=10, seed=0)
+             snapshot_every=10, seed=0, seconds_in_step=0.5)
 
 
 def serve_jobs(nb, rate, seconds, seed):
@@ -769,7 +780,11 @@ def main():
                     help="step: the 4M Barnes-Hut system; batch: 512 batched systems vs plain solves; "
                          "serve: a Poisson job stream through the job server vs plain solves")
     ap.add_argument("--serve-rate", type=float, default=SERVE["rate"])
-    ap.add_argument("--serve-seconds", type=float, default=SERVE["seconds"])
+    ap.add_argument("--serve-seconds", type=float, default=None,
+                    help=f"length of the job stream (default {SERVE['seconds']} s in serve mode, "
+                         f"{SERVE['seconds_in_step']} s beside the step bench)")
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="step mode: omit the direct-sum, batched and serving measurements")
     ap.add_argument("--skip-plain", action="store_true", help="serve mode: omit the plain-solve arm")
     ap.add_argument("--systems", type=int, default=BATCH["systems"])
     ap.add_argument("--batch-steps", type=int, default=BATCH["steps"])
@@ -784,11 +799,23 @@ def main():
         elif args.mode == "batch":
             out = run_batch(args, dist)
         elif args.mode == "serve":
+            if args.serve_seconds is None:
+                args.serve_seconds = SERVE["seconds"]
             out = run_serve(args, dist)
         elif args.mode == "direct":
             out = run_direct(args, dist)
         else:
             out = run_ours(args, dist)
+            if not args.skip_extras:
+                # the other measurements of the workload family, each its own
+                # timed region (see their modes): direct sum, batched systems
+                # against plain solves, the job server against plain solves
+                extra = {"direct": run_direct(args, dist), "batched": run_batch(args, dist)}
+                if args.serve_seconds is None:
+                    args.serve_seconds = SERVE["seconds_in_step"]
+                extra["serving"] = run_serve(args, dist)
+                if out is not None:
+                    out.update(extra)
         if dist.rank == 0 and out is not None:
             print(json.dumps(out), flush=True)
     finally:
