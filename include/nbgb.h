@@ -276,6 +276,22 @@ void nb_host_free(void *p);
 nb_status nb_direct_accel_noalloc(const float *d_body4, int32_t n, float eps, float G, float *d_acc4,
                                   void *stream);
 
+/* ---- snapshot files ----
+ * One system at one step: a 32-byte header (magic "NBSNAP01", uint32 version
+ * 1, uint32 N, int64 step, float64 simulated time) followed by float32
+ * positions[3N], velocities[3N], masses[N]; every field little-endian.  The
+ * reference keeps no files (its state lives in OpenCL buffers); this is the
+ * exchange format for snapshots of served jobs and of any handle.
+ * nb_snapshot_write: vel3 may be NULL (zeros are written).
+ * nb_snapshot_read: with all three arrays NULL only the header is read (*n,
+ * *step, *time); otherwise N must be <= capacity; any array may be NULL.
+ * nb_save_snapshot: the handle's current state (as nb_get_state). */
+nb_status nb_snapshot_write(const char *path, int64_t step, double time, const float *pos3, const float *vel3,
+                            const float *mass, int32_t n);
+nb_status nb_snapshot_read(const char *path, int64_t *step, double *time, float *pos3, float *vel3, float *mass,
+                           int32_t capacity, int32_t *n);
+nb_status nb_save_snapshot(nb_sim *sim, const char *path, int64_t step, double time);
+
 /* ---- batched systems ----
  * Many independent simulations of uneven N advanced together, each with its
  * own nb_config (the reference runs one CMyApp per simulation,

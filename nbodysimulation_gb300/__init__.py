@@ -121,6 +121,10 @@ SIGNATURES = {
     "nb_batch_autotune": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
     "nb_batch_info": ([_P, _P], _I),
     "nb_batch_last_error_message": ([_P], ctypes.c_char_p),
+    "nb_snapshot_write": ([ctypes.c_char_p, ctypes.c_int64, _D, _P, _P, _P, _I], _I),
+    "nb_snapshot_read": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_D), _P, _P, _P, _I,
+                          ctypes.POINTER(_I)], _I),
+    "nb_save_snapshot": ([_P, ctypes.c_char_p, ctypes.c_int64, _D], _I),
     "nb_server_config_default": ([_P], None),
     "nb_server_create": ([_P, _P, _P, ctypes.POINTER(_P)], _I),
     "nb_server_submit": ([_P, ctypes.POINTER(NbConfig), _I, _F, _P, _P, _P, ctypes.POINTER(ctypes.c_int64)], _I),
@@ -515,3 +519,34 @@ class Server:
         out = NbServerStats()
         self._check(self.L.nb_server_get_stats(self.h, ctypes.byref(out)), "nb_server_get_stats")
         return {k: getattr(out, k) for k, _ in NbServerStats._fields_ if k != "pad"}
+
+
+def write_snapshot(path, pos, mass, vel=None, step=0, time=0.0):
+    """Write one system's state in the snapshot format (nb_snapshot_write)."""
+    p = _f32(pos, (-1,))
+    m = _f32(mass, (-1,))
+    v = None if vel is None else _f32(vel, (-1,))
+    st = load().nb_snapshot_write(os.fsencode(path), int(step), float(time), p.ctypes.data,
+                                  None if v is None else v.ctypes.data, m.ctypes.data, len(m))
+    if st:
+        raise NbError(st, f"nb_snapshot_write {path}")
+
+
+def read_snapshot(path):
+    """(step, time, pos[N,3], vel[N,3], mass[N]) of a snapshot file."""
+    L = load()
+    n = ctypes.c_int32(0)
+    step = ctypes.c_int64(0)
+    t = ctypes.c_double(0.0)
+    st = L.nb_snapshot_read(os.fsencode(path), ctypes.byref(step), ctypes.byref(t), None, None, None, 0,
+                            ctypes.byref(n))
+    if st:
+        raise NbError(st, f"nb_snapshot_read {path}")
+    pos = np.zeros((n.value, 3), np.float32)
+    vel = np.zeros((n.value, 3), np.float32)
+    mass = np.zeros(n.value, np.float32)
+    st = L.nb_snapshot_read(os.fsencode(path), ctypes.byref(step), ctypes.byref(t), pos.ctypes.data,
+                            vel.ctypes.data, mass.ctypes.data, n.value, ctypes.byref(n))
+    if st:
+        raise NbError(st, f"nb_snapshot_read {path}")
+    return step.value, t.value, pos, vel, mass

@@ -181,3 +181,35 @@ def test_generated_initial_conditions_and_validation(gpu):
             srv.submit(jcfg(nb, 100, True), 0, 1e-3)
     ref = standalone(nb, cfg, 15, 1e-3, (pos, vel, mass))
     np.testing.assert_array_equal(got[0], ref[0])
+
+
+def test_snapshot_file_of_a_handle_and_of_a_job(gpu, tmp_path):
+    nb = gpu
+    cfg = jcfg(nb, 3000, True)
+    state = job_state(3000, 21)
+    with nb.Simulation(cfg) as s:
+        s.set_state(state[0], state[2], state[1])
+        s.step(1e-3, 4)
+        p, v, _, m = s.get_state()
+        path = tmp_path / "h.nbsnap"
+        assert nb.load().nb_save_snapshot(s.h, str(path).encode(), 4, 4e-3) == 0
+    step, t, p2, v2, m2 = nb.read_snapshot(path)
+    assert step == 4 and abs(t - 4e-3) < 1e-15
+    np.testing.assert_array_equal(p2, p)
+    np.testing.assert_array_equal(v2, v)
+    np.testing.assert_array_equal(m2, m)
+    # a served job's snapshot, written from the callback, reads back as delivered
+    got = {}
+
+    def on_event(job, event, value, pos, vel):
+        if event == nb.JOB_EVENT_SNAPSHOT and value == 10:
+            nb.write_snapshot(tmp_path / "j.nbsnap", pos, state[2], step=value, time=value * 1e-3)
+            got["pos"] = pos
+
+    with nb.Server(on_event=on_event) as srv:
+        j = srv.submit(cfg, 12, 1e-3, state[0], state[2], state[1])
+        assert srv.wait(j, WAIT_S) == 0
+    step, _, p3, _, _ = nb.read_snapshot(tmp_path / "j.nbsnap")
+    assert step == 10
+    np.testing.assert_array_equal(p3, got["pos"])
+    np.testing.assert_array_equal(p3, standalone(nb, cfg, 10, 1e-3, state)[0])
