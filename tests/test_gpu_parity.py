@@ -334,3 +334,34 @@ def test_coincident_bodies_do_not_hang(gpu):
     sim = bh_sim(nb, pos, masses(n, 3), 0.5, 0.01)
     st = sim.step(1e-3, 1, check=False)
     assert st in (nb.ERR_DEPTH, nb.ERR_CELL_OVERFLOW)
+
+
+def test_tree_after_steps_equals_the_oracle(gpu, oracle):
+    """After steps (integrated positions, buffers flipped, the previous tree
+    overwritten) the tree (octant paths), the summaries and the sort equal
+    the oracle's build on the same positions, bit for bit."""
+    nb = gpu
+    n = 30000
+    pos = normal(n, 77, (1.0, 1.0, 0.2))
+    mass = masses(n, 77, "lognormal")
+    sim = bh_sim(nb, pos, mass, 0.5, 0.005)
+    sim.step(1e-3, 2)
+    cur = sim.get_state()[0]
+    sim.step(0.0, 1)  # positions unchanged: the tree of `cur`
+    box = sim.stage_debug(nb.DEBUG_BBOX)
+    info = sim.stage_debug(nb.DEBUG_TREE_INFO)
+    cap = int(info[1])
+    t = oracle.tree_build(oracle.SEM_GEOMETRIC, cur, mass, box, cap)
+    children = sim.stage_debug(nb.DEBUG_CHILDREN)
+    pg, dg, fg = oracle.tree_paths(children, n, n + cap)
+    po, do, fo = oracle.tree_paths(t.children, n, t.root)
+    assert fg == n and np.array_equal(pg, po) and np.array_equal(dg, do)
+    octant_children = t.children.copy()
+    assert oracle.saturate(t) == 0
+    tg = cell_table(children, sim.stage_debug(nb.DEBUG_NODE_MASS), sim.stage_debug(nb.DEBUG_NODE_POS),
+                    sim.stage_debug(nb.DEBUG_BODY_COUNT), n, n + cap)
+    to = cell_table(octant_children, t.mass, t.pos, t.body_count, n, t.root)
+    assert tg == to
+    srt_o, _ = oracle.sort_bodies(t.children, n, t.root)
+    assert np.array_equal(sim.stage_debug(nb.DEBUG_SORTED), srt_o)
+    sim.close()
