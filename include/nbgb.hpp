@@ -194,4 +194,90 @@ private:
     float elapsed_ = 0.0f;
 };
 
+// Many simulations stepped together (nb_batch_*); no counterpart in the
+// reference, which runs one CMyApp per simulation.
+class Batch {
+public:
+    explicit Batch(const std::vector<SimulationConfig> &configs) {
+        std::vector<nb_config> c;
+        for (const auto &sc : configs) c.push_back(sc.ToC());
+        for (const auto &x : c) sizes_.push_back(x.num_of_bodies);
+        check(nb_batch_create(c.data(), (int32_t)c.size(), &b_), "nb_batch_create");
+    }
+    ~Batch() {
+        if (b_) nb_batch_destroy(b_);
+    }
+    Batch(const Batch &) = delete;
+    Batch &operator=(const Batch &) = delete;
+
+    size_t Size() const { return sizes_.size(); }
+    void SetState(int k, const std::vector<float> &pos3, const std::vector<float> &vel3,
+                  const std::vector<float> &mass) {
+        step_check(nb_batch_set_state(b_, k, pos3.data(), vel3.empty() ? nullptr : vel3.data(), mass.data()),
+                   "nb_batch_set_state");
+    }
+    void GetState(int k, std::vector<float> &pos3, std::vector<float> &vel3) {
+        const size_t n = (size_t)sizes_.at(k);
+        pos3.resize(3 * n);
+        vel3.resize(3 * n);
+        step_check(nb_batch_get_state(b_, k, pos3.data(), vel3.data(), nullptr, nullptr), "nb_batch_get_state");
+    }
+    int Autotune(const char *cache_path) {
+        int32_t v = -1;
+        step_check(nb_batch_autotune(b_, cache_path, &v), "nb_batch_autotune");
+        return v;
+    }
+    void Step(float dt, int nsteps) { step_check(nb_batch_step(b_, dt, nsteps), "nb_batch_step"); }
+    nb_status SystemStatus(int k) { return nb_batch_system_status(b_, k); }
+    nb_batch *Handle() { return b_; }
+
+private:
+    void step_check(nb_status s, const char *what) {
+        if (s != NB_OK) throw Error(s, std::string(what) + ": " + nb_batch_last_error_message(b_));
+    }
+    nb_batch *b_ = nullptr;
+    std::vector<int> sizes_;
+};
+
+// Job server (nb_server_*): continuous batching of simulation jobs; events
+// arrive on a library thread.
+class Server {
+public:
+    using Callback = void (*)(void *user, int64_t job, int32_t event, int32_t value, const float *pos3,
+                              const float *vel3, int32_t n);
+    explicit Server(const nb_server_config *cfg = nullptr, Callback fn = nullptr, void *user = nullptr) {
+        nb_server_config c;
+        if (cfg) c = *cfg;
+        else nb_server_config_default(&c);
+        check(nb_server_create(&c, fn, user, &s_), "nb_server_create");
+    }
+    ~Server() {
+        if (s_) nb_server_destroy(s_);
+    }
+    Server(const Server &) = delete;
+    Server &operator=(const Server &) = delete;
+
+    // initial conditions generated from the config when pos3 is empty
+    int64_t Submit(const SimulationConfig &sc, int steps, float dt, const std::vector<float> &pos3 = {},
+                   const std::vector<float> &vel3 = {}, const std::vector<float> &mass = {}) {
+        nb_config c = sc.ToC();
+        int64_t job = -1;
+        const nb_status s =
+            nb_server_submit(s_, &c, steps, dt, pos3.empty() ? nullptr : pos3.data(),
+                             vel3.empty() ? nullptr : vel3.data(), mass.empty() ? nullptr : mass.data(), &job);
+        if (s != NB_OK) throw Error(s, "nb_server_submit");
+        return job;
+    }
+    nb_status Wait(int64_t job = -1, double timeout_s = -1.0) { return nb_server_wait(s_, job, timeout_s); }
+    nb_server_stats Stats() {
+        nb_server_stats st;
+        nb_server_get_stats(s_, &st);
+        return st;
+    }
+    nb_server *Handle() { return s_; }
+
+private:
+    nb_server *s_ = nullptr;
+};
+
 }  // namespace nb

@@ -177,6 +177,20 @@ int main() {
         std::vector<float> p, v, m;
         app.GetState(p, v, m);
         std::printf("stepped %zu\n", m.size());
+        // several simulations in one batch, and a job server
+        nb::SimulationConfig d = c;
+        d.SetNumberOfBodies(3000);
+        d.SetAlgorithmConfig(nb::BRUTE_FORCE_LOCAL);
+        nb::Batch batch({c, d});
+        batch.SetState(0, p, v, m);
+        batch.Step(1e-3f, 2);
+        std::vector<float> bp, bv;
+        batch.GetState(0, bp, bv);
+        std::printf("batched %zu %zu\n", batch.Size(), bp.size() / 3);
+        nb::Server server;
+        const int64_t job = server.Submit(c, 12, 1e-3f);
+        const nb_status ws = server.Wait(job, 60.0);
+        std::printf("served %d %lld\n", (int)ws, (long long)server.Stats().completed);
     } catch (const nb::Error &e) {
         std::printf("error %d\n", (int)e.status);
     }
@@ -198,3 +212,22 @@ def test_cpp_host_mirror_compiles_and_links(nbgb_lib, tmp_path):
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     assert r.stdout.startswith("stepped 1024") or r.stdout.strip() in (f"error {nbgb_lib.ERR_NO_DEVICE}",
                                                                           f"error {nbgb_lib.ERR_CUDA}")
+    if r.stdout.startswith("stepped"):
+        assert "batched 2 1024" in r.stdout and "served 0 1" in r.stdout, r.stdout
+
+
+@pytest.mark.gpu
+def test_cpp_host_mirror_on_gpu(gpu, tmp_path):
+    """The same C++ program on a GPU: one CMyApp-style step, a batch of two
+    systems and one served job."""
+    nb = gpu
+    src = tmp_path / "app.cpp"
+    src.write_text(CPP_PROGRAM)
+    exe = tmp_path / "app"
+    libdir = os.path.dirname(nb.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lnbgb",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert r.stdout.startswith("stepped 1024"), r.stdout
+    assert "batched 2 1024" in r.stdout and "served 0 1" in r.stdout, r.stdout
