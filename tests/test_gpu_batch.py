@@ -177,3 +177,23 @@ def test_many_small_systems(gpu):
             p = b.get_state(k)[0]
             assert np.all(np.isfinite(p))
             assert np.max(np.abs(p - states[k][0])) < 0.05
+
+
+def test_more_systems_than_one_scan_block(gpu):
+    """1100 tree systems: the used-cell scan runs over more systems than its
+    1024 threads (two chunks with a carry); every system equals its
+    standalone step (checked on a sample that spans both chunks)."""
+    nb = gpu
+    rng = np.random.default_rng(11)
+    sizes = [int(x) for x in rng.integers(64, 600, size=1100)]
+    cfgs = [cfg(nb, n, True) for n in sizes]
+    states = [(normal(n, 3000 + k), lognormal_mass(n, 3000 + k), small_vel(n, 3000 + k))
+              for k, n in enumerate(sizes)]
+    with nb.Batch(cfgs) as b:
+        for k, (p, m, v) in enumerate(states):
+            b.set_state(k, p, m, v)
+        b.step(1e-3, 2)
+        for k in (0, 1023, 1024, 1099):
+            ref = standalone(nb, cfgs[k], *states[k], 1e-3, 2)
+            np.testing.assert_array_equal(b.get_state(k)[0], ref[0])
+            np.testing.assert_array_equal(b.get_state(k)[1], ref[1])

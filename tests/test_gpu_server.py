@@ -213,3 +213,33 @@ def test_snapshot_file_of_a_handle_and_of_a_job(gpu, tmp_path):
     assert step == 10
     np.testing.assert_array_equal(p3, got["pos"])
     np.testing.assert_array_equal(p3, standalone(nb, cfg, 10, 1e-3, state)[0])
+
+
+def test_nonfinite_job_fails_alone(gpu):
+    """A job with a NaN position fails with NB_ERR_NONFINITE; a job beside it
+    is unaffected."""
+    nb = gpu
+    bad_state = job_state(4000, 31)
+    bad_state[0][17, 1] = np.nan
+    good = (jcfg(nb, 4000, True), 15, job_state(4000, 32))
+    with nb.Server() as srv:
+        bad = srv.submit(jcfg(nb, 4000, True), 15, 1e-3, bad_state[0], bad_state[2], bad_state[1])
+        ok = srv.submit(good[0], good[1], 1e-3, good[2][0], good[2][2], good[2][1])
+        assert srv.wait(bad, WAIT_S) == 7  # NB_ERR_NONFINITE
+        assert srv.wait(ok, WAIT_S) == 0
+        np.testing.assert_array_equal(srv.result(ok, 4000)[0], standalone(nb, *good[:2], 1e-3, good[2])[0])
+
+
+def test_destroy_with_jobs_in_flight(gpu):
+    """Destroying the server while jobs are queued and running cancels them
+    and returns; nothing is left on the device."""
+    nb = gpu
+    srv = nb.Server(max_jobs=2)
+    for k in range(6):
+        n = 20000 + 1000 * k
+        st = job_state(n, 50 + k)
+        srv.submit(jcfg(nb, n, True), 300, 1e-3, st[0], st[2], st[1])
+    time.sleep(0.05)
+    t0 = time.time()
+    srv.close()
+    assert time.time() - t0 < 60
