@@ -52,6 +52,7 @@ WORKLOAD = dict(name="bh_plummer_n4m_theta0.5", n=4194304, sigma=(1.0, 1.0, 0.2)
                 eps=0.005, dt=1e-3, G=1.0, precision="compensated", multipole="quadrupole")
 PROBE_SAMPLES = 8192
 FP32_LANES_PER_SM = 128
+MUFU_LANES_PER_SM = 16  # rsqrt results per SM per clock
 FLOPS_PER_INTERACTION = 12  # FP32 ops per monopole interaction (3 sub, 3 fma, 3 mul, 3 fma)
 FORCE_DRAM_BYTES_PER_BODY = (387.995392e6 + 75.690752e6) / 1048576  # dram read + write, k_force, N = 1M
 FLOPS_PER_QUADRUPOLE = 19   # extra FP32 ops per cell quadrupole term (Q.d 9, d.Q.d 3, r^5 r^7 2, 2.5*sq 1, 4 fma)
@@ -449,6 +450,7 @@ def direct_leg(nb, dev, n, tiled, eps, steps, warmup, sm_count, sm_mhz):
                          "frac": ips / peak_ips,
                          "peak_kind": "derived: 128 FP32 lanes x SMs x maximum SM clock"},
             "gflops_20_per_pair": ips * 20 / 1e9,
+            "mufu_frac": ips / (MUFU_LANES_PER_SM * sm_count * sm_mhz * 1e6),
             "accuracy": {"rms_rel_err": err_rms, "max_rel_err": err_max, "samples": int(len(sample)),
                          "oracle": "FP64 direct sum on the GPU"}}
 
