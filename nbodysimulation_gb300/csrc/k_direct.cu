@@ -86,22 +86,35 @@ __device__ __forceinline__ void integrate_one(const DevSim &s, const StepParams 
 
 // ---------------------------------------------------------------------------
 // direct_global: one thread per body, j straight from global memory through
-// L1 (update, brute_force_update.cl:3-105).  The naive baseline.
+// L1 (update, brute_force_update.cl:3-105), no shared-memory staging.  When
+// the bodies alone do not fill the GPU (the reference runs this variant at
+// N = 4096: 32 blocks for 152 SMs), gridDim.y blocks split the j range and
+// add partial accelerations into `part` (float atomics) for a separate
+// integrate pass.
 // ---------------------------------------------------------------------------
+constexpr int kGlobalThreads = 128;
 template <int kMethod, bool kQuirk, bool kEpsZero>
-__global__ void __launch_bounds__(256) k_direct_global(DevSim s, StepParams p, float eps) {
+__global__ void __launch_bounds__(kGlobalThreads) k_direct_global(DevSim s, StepParams p, float eps, float4 *part) {
     const int n = s.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const int per = (n + gridDim.y - 1) / gridDim.y;
+    const int j0 = blockIdx.y * per, j1 = min(n, j0 + per);
     const float4 me = s.body_cur[i];
     const float eps2 = eps * eps;
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
-    for (int j = 0; j < n; ++j) {
+    for (int j = j0; j < j1; ++j) {
         const float4 q = __ldg(&s.body_cur[j]);
         if (!kQuirk && kEpsZero && j == i) continue;
         pair<kQuirk, false>(me, q, eps2, ax, ay, az);
     }
-    integrate_one<kMethod>(s, p, i, me, ax * p.G, ay * p.G, az * p.G);
+    if (gridDim.y == 1) {
+        integrate_one<kMethod>(s, p, i, me, ax * p.G, ay * p.G, az * p.G);
+    } else {
+        atomicAdd(&part[i].x, ax);
+        atomicAdd(&part[i].y, ay);
+        atomicAdd(&part[i].z, az);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -354,7 +367,17 @@ static cudaError_t launch_direct_t(const DevSim &s, const StepParams &p, float e
                                    cudaStream_t st, float4 *part) {
     const int n = s.n;
     if (!tiled) {
-        k_direct_global<kMethod, kQuirk, kEpsZero><<<(n + 255) / 256, 256, 0, st>>>(s, p, eps);
+        const int bx = (n + kGlobalThreads - 1) / kGlobalThreads;
+        int split = (sm_count * 6 + bx - 1) / bx;
+        if (split > (n + 63) / 64) split = (n + 63) / 64;  // at least 64 j per block
+        if (split <= 1) {
+            k_direct_global<kMethod, kQuirk, kEpsZero><<<dim3(bx, 1), kGlobalThreads, 0, st>>>(s, p, eps, part);
+            return cudaGetLastError();
+        }
+        cudaError_t e = cudaMemsetAsync(part, 0, sizeof(float4) * (size_t)n, st);
+        if (e != cudaSuccess) return e;
+        k_direct_global<kMethod, kQuirk, kEpsZero><<<dim3(bx, split), kGlobalThreads, 0, st>>>(s, p, eps, part);
+        k_integrate_partial<kMethod><<<(n + 255) / 256, 256, 0, st>>>(s, p, part);
         return cudaGetLastError();
     }
     // bodies per thread: the most that still gives at least six blocks per
