@@ -687,16 +687,16 @@ void orc_direct_quirk_global(const float *pos3, const float *mass, int n, float 
 }
 
 /* update_local (kernels/brute_force_update.cl:144-185), eps 0.1.
- * q12 != 0 restates the tile schedule as written, defined for
+ * tile_schedule != 0 restates the tile schedule as written, defined for
  * n % wg == 0: iteration 0 loads tile 0 and skips j == i; iteration t >= 1
  * loads tile t-1 and skips slot j when i == t*wg + j; N/wg + 1 iterations.
- * q12 == 0: every j != i once, ascending. */
-int orc_direct_quirk_local(const float *pos3, const float *mass, int n, int wg, int q12, float G, float *acc3) {
-    if (q12 && (wg <= 0 || n % wg != 0)) return ORC_ERR_ARG;
+ * tile_schedule == 0: every j != i once, ascending. */
+int orc_direct_quirk_local(const float *pos3, const float *mass, int n, int wg, int tile_schedule, float G, float *acc3) {
+    if (tile_schedule && (wg <= 0 || n % wg != 0)) return ORC_ERR_ARG;
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
         float a[3] = {0.0f, 0.0f, 0.0f};
-        if (!q12) {
+        if (!tile_schedule) {
             for (int j = 0; j < n; ++j)
                 if (j != i) orc_quirk_pair(pos3 + i * 3, pos3 + j * 3, mass[j], 0.1f, a);
         } else {
@@ -764,10 +764,10 @@ void orc_integrate(int method, int primed, int n, float dt, const float *acc_new
 /* calc_collision_traj (:3-15): if |pi - pj| > ri + rj keep v, else reflect
  * v <- v - 2 dot(n, v) n with n = normalize(pj - pi).  Reflections apply in
  * j order to the running v_i; positions are read-only.  Radii are 0.015
- * (:59,65).  q12 != 0 uses update_local's tile schedule as written (n % wg == 0);
+ * (:59,65).  tile_schedule != 0 uses update_local's tile schedule as written (n % wg == 0);
  * otherwise every j != i once, ascending. */
-int orc_collision(const float *pos3, float *vel3, int n, int wg, int q12) {
-    if (q12 && (wg <= 0 || n % wg != 0)) return ORC_ERR_ARG;
+int orc_collision(const float *pos3, float *vel3, int n, int wg, int tile_schedule) {
+    if (tile_schedule && (wg <= 0 || n % wg != 0)) return ORC_ERR_ARG;
     const float rr = 0.015f + 0.015f;
     float *out = (float *)malloc(sizeof(float) * 3 * (size_t)n);
     if (!out) return ORC_ERR_ARG;
@@ -775,13 +775,13 @@ int orc_collision(const float *pos3, float *vel3, int n, int wg, int q12) {
     for (int i = 0; i < n; ++i) {
         const float *pi = pos3 + i * 3;
         float v[3] = {vel3[i * 3 + 0], vel3[i * 3 + 1], vel3[i * 3 + 2]};
-        int iters = q12 ? n / wg + 1 : 1;
+        int iters = tile_schedule ? n / wg + 1 : 1;
         for (int t = 0; t < iters; ++t) {
             int tile = t == 0 ? 0 : t - 1;
-            int jn = q12 ? wg : n;
+            int jn = tile_schedule ? wg : n;
             for (int j = 0; j < jn; ++j) {
                 int b;
-                if (q12) {
+                if (tile_schedule) {
                     if (i == t * wg + j) continue;
                     b = tile * wg + j;
                 } else {

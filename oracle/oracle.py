@@ -217,12 +217,12 @@ def direct_quirk_global(pos3, mass, G):
     return acc
 
 
-def direct_quirk_local(pos3, mass, G, wg=0, q12=False):
+def direct_quirk_local(pos3, mass, G, wg=0, tile_schedule=False):
     pos3 = f32(pos3).reshape(-1, 3)
     acc = np.zeros_like(pos3)
-    rc = lib().orc_direct_quirk_local(_p(pos3), _p(f32(mass)), pos3.shape[0], wg, 1 if q12 else 0, G, _p(acc))
+    rc = lib().orc_direct_quirk_local(_p(pos3), _p(f32(mass)), pos3.shape[0], wg, 1 if tile_schedule else 0, G, _p(acc))
     if rc:
-        raise ValueError("q12 schedule needs n % wg == 0")
+        raise ValueError("tile_schedule schedule needs n % wg == 0")
     return acc
 
 
@@ -237,12 +237,12 @@ def integrate(method, pos3, vel3, acc_new3, accs3, dt, primed=False):
     return pos3, vel3, accs3
 
 
-def collision(pos3, vel3, wg=0, q12=False):
+def collision(pos3, vel3, wg=0, tile_schedule=False):
     pos3 = f32(pos3).reshape(-1, 3)
     v = f32(vel3).reshape(-1, 3).copy()
-    rc = lib().orc_collision(_p(pos3), _p(v), pos3.shape[0], wg, 1 if q12 else 0)
+    rc = lib().orc_collision(_p(pos3), _p(v), pos3.shape[0], wg, 1 if tile_schedule else 0)
     if rc:
-        raise ValueError("q12 schedule needs n % wg == 0")
+        raise ValueError("tile_schedule schedule needs n % wg == 0")
     return v
 
 

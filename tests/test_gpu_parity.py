@@ -192,7 +192,7 @@ def test_direct_against_oracle(gpu, oracle, algo, quirk, n):
     if quirk:
         # the reference's arithmetic; the GPU visits every j once (no tile-0 reload)
         acc_o = oracle.direct_quirk_global(pos, mass, 1.0) if algo == 1 else \
-            oracle.direct_quirk_local(pos, mass, 1.0, q12=False)
+            oracle.direct_quirk_local(pos, mass, 1.0, tile_schedule=False)
     else:
         acc_o = oracle.direct_fp32(pos, mass, 0.05, 1.0)
     err = rel_to_typical(acc_g, acc_o)

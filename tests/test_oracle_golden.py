@@ -90,7 +90,7 @@ def test_direct_quirk_and_euler(oracle, name):
     g = load(name)
     wg = int(g["wg"])
     assert np.array_equal(oracle.direct_quirk_global(g["pos"], g["mass"], 1.0), g["acc_global"])
-    assert np.array_equal(oracle.direct_quirk_local(g["pos"], g["mass"], 1.0, wg=wg, q12=True), g["acc_local"])
+    assert np.array_equal(oracle.direct_quirk_local(g["pos"], g["mass"], 1.0, wg=wg, tile_schedule=True), g["acc_local"])
     a = oracle.direct_quirk_global(g["pos"], g["mass"], 1.0)
     p, v, _ = oracle.integrate(oracle.EULER, g["pos"], g["vel"], a, np.zeros_like(a), 1e-3)
     assert np.array_equal(p, g["euler_pos"]) and np.array_equal(v, g["euler_vel"])
@@ -99,7 +99,7 @@ def test_direct_quirk_and_euler(oracle, name):
 @pytest.mark.parametrize("name", DIRECT_CASES)
 def test_collision_and_copy(oracle, name):
     g = load(name)
-    v = oracle.collision(g["coll_pos"], g["vel"], wg=int(g["wg"]), q12=True)
+    v = oracle.collision(g["coll_pos"], g["vel"], wg=int(g["wg"]), tile_schedule=True)
     assert np.array_equal(v, g["coll_vel"])
     assert np.any(v != g["vel"])  # the fixture does collide
     assert np.array_equal(oracle.copy_vertices(g["coll_pos"]), g["verts"])

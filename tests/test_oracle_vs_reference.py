@@ -65,9 +65,9 @@ def test_direct_and_collision_live(oracle, n, wg):
                           oracle.direct_quirk_global(pos, mass, 1.0))
     rs.set_bodies(pos.ravel(), mass)
     assert np.array_equal(rs.accelerations_via_leapfrog(0, 0, 1.0, "local"),
-                          oracle.direct_quirk_local(pos, mass, 1.0, wg=wg, q12=True))
+                          oracle.direct_quirk_local(pos, mass, 1.0, wg=wg, tile_schedule=True))
     cpos, _ = bodies(n, 32, scale=0.05)
     vel = (np.random.default_rng(3).normal(size=(n, 3)) * 0.1).astype(np.float32)
     rs.set_bodies(cpos.ravel(), mass, vel.ravel(), None)
     rs.collision()
-    assert np.array_equal(rs.get(rs.VEL, np.float32).reshape(n, 3), oracle.collision(cpos, vel, wg=wg, q12=True))
+    assert np.array_equal(rs.get(rs.VEL, np.float32).reshape(n, 3), oracle.collision(cpos, vel, wg=wg, tile_schedule=True))
