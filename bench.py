@@ -233,6 +233,34 @@ def cpu_baseline(pos, mass, sample_groups=512, repeats=1):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+def stage_roofline(stage_ms, n, cells, hbm_gbs, quad=True):
+    """Algorithmic bytes of every Barnes-Hut stage (each datum moved once)
+    over its CUDA-event time, against the measured HBM copy rate.  N bodies,
+    C = cells the tree allocated; layout as in the library (float4 bodies,
+    8-int child rows, packed child lines)."""
+    model = {
+        # body {x,y,z,m} read
+        "bbox": 16 * n,
+        # body read; per cell: child row 32 B, parent/arrive/start 12 B written
+        "build": 16 * n + 44 * cells,
+        # per cell: child row read; every body and cell {x,y,z,m} read once;
+        # compacted row 32, packed line 128, centre/mass 16, count 4 written,
+        # with quadrupoles cell moments 32 and packed moments 192 more
+        "summarize": 32 * cells + 16 * (n + cells) + (180 + (224 if quad else 0)) * cells,
+        # per cell: compacted row 32 + child counts 4 read, start 4 written;
+        # sorted index 4 per body written
+        "sort": 40 * cells + 4 * n,
+        "force": 84 * n + (352 if quad else 160) * cells,
+    }
+    out = {}
+    for k, b in model.items():
+        ms = stage_ms.get(k) or 0.0
+        gbs = b / (ms / 1e3) / 1e9 if ms > 0 else None
+        out[k] = {"ms": ms, "algorithmic_bytes": b, "achieved_gbs": gbs,
+                  "frac_of_hbm": (gbs / hbm_gbs) if gbs else None}
+    return out
+
+
 def run_ours(args, dist: Dist):
     from nbodysimulation_gb300 import build as nbbuild
     if dist.local_rank == 0:
@@ -366,6 +394,7 @@ def run_ours(args, dist: Dist):
                     "ops_model": "12 FP32 ops per interaction + 19 per cell quadrupole term",
                     "peak_kind": "derived: 128 FP32 lanes x SMs x maximum SM clock"},
         "tree": {"cells_used": cells_used, "max_depth": int(info[3])},
+        "stages_roofline": stage_roofline(stage, n, cells_used, peaks["hbm_gbs"]),
         "clocks": clk,
     }
     if not args.skip_cpu:
