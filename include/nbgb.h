@@ -243,6 +243,14 @@ nb_status nb_force_error_probe(nb_sim *sim, const int32_t *sample, int32_t ns, d
  * potential energy (FP64 pair sum; computed only when with_potential != 0). */
 nb_status nb_diagnostics(nb_sim *sim, int32_t with_potential, double out[9]);
 
+/* ---- failure-path test hook ----
+ * Caps the iterations of the tree stages' bounded waits (the build's lock
+ * retries and the sort's wait for a parent's start) at `cap` (0 restores the
+ * default, 2^24).  With a tiny cap a step gives up with NB_ERR_SPIN_TIMEOUT
+ * instead of waiting, keeps its step-start state, and the handle stays
+ * usable: the way the timeout path is exercised without hanging a GPU. */
+nb_status nb_debug_set_spin_cap(nb_sim *sim, int32_t cap);
+
 /* ---- last error ---- */
 nb_status nb_last_error(const nb_sim *sim);
 const char *nb_last_error_message(const nb_sim *sim);

@@ -101,6 +101,7 @@ SIGNATURES = {
     "nb_kernel_launches": ([_P], ctypes.c_int64),
     "nb_time_steps": ([_P, _F, _I, ctypes.POINTER(_F)], _I),
     "nb_get_work_counters": ([_P, _P], _I),
+    "nb_debug_set_spin_cap": ([_P, _I], _I),
     "nb_get_device_view": ([_P, ctypes.POINTER(NbDeviceView)], _I),
     "nb_set_state_device": ([_P, _P, _P, _P], _I),
     "nb_get_state_device": ([_P, _P, _P], _I),
@@ -291,6 +292,10 @@ class Simulation:
         out = np.zeros(3, np.uint64)
         self._check(self.L.nb_get_work_counters(self.h, out.ctypes.data), "nb_get_work_counters")
         return int(out[0]), int(out[1]), int(out[2])
+
+    def set_spin_cap(self, cap):
+        """Test hook: cap the tree stages' bounded waits (0 = default)."""
+        self._check(self.L.nb_debug_set_spin_cap(self.h, cap), "nb_debug_set_spin_cap")
 
     def kernel_launches(self):
         return int(self.L.nb_kernel_launches(self.h))

@@ -11,6 +11,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/nbgb.h"
 #include "nbgb_internal.cuh"
 
@@ -390,8 +392,18 @@ static nb_status enqueue_step(nb_sim *s, float dt, int timed) {
     p.quadrupole = s->quad ? 1 : 0;
     DevSim d = dev_view(s);
     cudaStream_t st = s->stream;
+    // profiling: CUDA events between the stages of the timed steps, and an
+    // NVTX range per stage for a timeline tool (free when none is attached)
+    static const char *const kStageName[] = {"nbgb bbox", "nbgb build", "nbgb summarize", "nbgb sort",
+                                             "nbgb force", "nbgb collision", "nbgb end"};
+    bool open_range = false;
     auto mark = [&](int k) {
         if (timed >= 0) cudaEventRecord(s->ev[(size_t)timed * (kNumStages + 1) + k], st);
+        if (s->profiling) {
+            if (open_range) nvtxRangePop();
+            open_range = k < 6;
+            if (open_range) nvtxRangePushA(s->tree ? kStageName[k] : "nbgb direct");
+        }
     };
     for (int k = 0; k < kNumStages; ++k) s->stage_ran[k] = false;
     if (s->tree) {
@@ -523,6 +535,14 @@ nb_status nb_time_steps(nb_sim *s, float dt, int32_t nsteps, float *total_ms) {
     NB_CUDA(s, cudaEventElapsedTime(&ms, s->t_begin, s->t_end));
     *total_ms = ms;
     return r;
+}
+
+nb_status nb_debug_set_spin_cap(nb_sim *s, int32_t cap) {
+    if (!s || cap < 0) return NB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->dev);
+    NB_CUDA(s, cudaMemcpyAsync(&s->ctrl->spin_cap, &cap, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    NB_CUDA(s, cudaStreamSynchronize(s->stream));
+    return NB_OK;
 }
 
 nb_status nb_get_work_counters(nb_sim *s, uint64_t out[3]) {

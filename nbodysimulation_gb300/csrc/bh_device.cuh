@@ -68,7 +68,7 @@ struct RefBox {  // the reference: calculateOctantIdx / adjustBoundaryValues
 // counter with warp-aggregated atomicSub (one atomic per converged group of
 // splitting threads).  A fresh cell's eight slots, parent link, arrival
 // counter and sort start are set by the allocating thread before
-// publication.  Retries are bounded (kSpinCap) and watch the status word; a
+// publication.  Retries are bounded (tree_spin_cap) and watch the status word; a
 // cell overflow or an over-deep chain restores the locked slot and records
 // the status.  Returns the body's depth, or -1 when the build must stop.
 //
@@ -77,7 +77,7 @@ struct RefBox {  // the reference: calculateOctantIdx / adjustBoundaryValues
 // bounding box; boxes halve as adjustBoundaryValues does.
 // ---------------------------------------------------------------------------
 template <class Geo, bool kRef>
-__device__ __forceinline__ int insert_body(const DevSim &s, const Geo &root_g, int i) {
+__device__ __forceinline__ int insert_body(const DevSim &s, const Geo &root_g, int i, long long spin_cap) {
     Ctrl *ctrl = s.ctrl;
     const int n = s.n, root = n + s.cap;
     const float4 P = s.body_cur[i];
@@ -148,7 +148,7 @@ __device__ __forceinline__ int insert_body(const DevSim &s, const Geo &root_g, i
                 return depth;
             }
         }
-        if (++spins > kSpinCap) {
+        if (++spins > spin_cap) {
             set_status(ctrl, kStSpinTimeout, i);
             return -1;
         }
@@ -294,7 +294,7 @@ __device__ __forceinline__ void summarize_from(const DevSim &s, int k) {
 // of counts in slot order) and place each child body.  Returns false when
 // the sort must stop (the status word is set).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool sort_cell(const DevSim &s, int k) {
+__device__ __forceinline__ bool sort_cell(const DevSim &s, int k, long long spin_cap) {
     Ctrl *ctrl = s.ctrl;
     const int n = s.n;
     const int c = k - n;
@@ -302,7 +302,7 @@ __device__ __forceinline__ bool sort_cell(const DevSim &s, int k) {
     long long spins = 0;
     unsigned pause = 32;  // back off: many waiting threads must not flood L2 with polls
     while (st < 0) {
-        if (++spins > kSpinCap) {
+        if (++spins > spin_cap) {
             set_status(ctrl, kStSpinTimeout, k);
             return false;
         }

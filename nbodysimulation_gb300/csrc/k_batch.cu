@@ -95,8 +95,9 @@ __device__ __forceinline__ int build_chunk(const DevSim &s, int i0, int i1) {
     load_box(s.ctrl, box);
     const Geo root_g = Geo::root(box);
     int local_max = 0;
+    const long long cap = tree_spin_cap(s.ctrl);
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        const int depth = insert_body<Geo, kRef>(s, root_g, i);
+        const int depth = insert_body<Geo, kRef>(s, root_g, i, cap);
         if (depth < 0) return -1;
         local_max = max(local_max, depth);
     }
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(256) k_batch_sort(BatchTables t) {
         const SysDesc &d = t.sys[k];
         const DevSim s = system_view(d);
         if (read_status(s.ctrl)) continue;
-        sort_cell(s, s.n + s.cap - (x - t.used_prefix[k]));
+        sort_cell(s, s.n + s.cap - (x - t.used_prefix[k]), tree_spin_cap(s.ctrl));
     }
 }
 

@@ -89,9 +89,10 @@ __global__ void __launch_bounds__(256) k_build(DevSim s) {
     load_box(ctrl, box);
     const Geo root_g = Geo::root(box);
     int local_max = 0;
+    const long long cap = tree_spin_cap(ctrl);
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += stride) {
-        const int depth = insert_body<Geo, kRef>(s, root_g, i);
+        const int depth = insert_body<Geo, kRef>(s, root_g, i, cap);
         if (depth < 0) return;
         local_max = max(local_max, depth);
     }
@@ -125,9 +126,10 @@ __global__ void __launch_bounds__(256) k_sort(DevSim s) {
     if (read_status(ctrl)) return;
     const int root = s.n + s.cap;
     const int bottom = ctrl->bottom;
+    const long long cap = tree_spin_cap(ctrl);
     const int stride = gridDim.x * blockDim.x;
     for (int k = root - (int)(blockIdx.x * blockDim.x + threadIdx.x); k >= bottom; k -= stride)
-        if (!sort_cell(s, k)) return;
+        if (!sort_cell(s, k, cap)) return;
 }
 
 // ---------------------------------------------------------------------------

@@ -41,7 +41,8 @@ struct Ctrl {
     int parity;            // batched systems: which body buffer is current
     int kdk_primed;        // batched systems: a KDK half-kick has happened
     int budget;            // batched systems: steps left (< 0 unlimited, 0 inert)
-    int pad0[2];
+    int spin_cap;          // > 0: iteration cap of the tree stages' waits (a test hook); 0: kSpinCap
+    int pad0[1];
     // cleared by the host once per nb_step call (everything from here on)
     int status;
     int status_info;
@@ -113,6 +114,15 @@ __device__ __forceinline__ int read_status(const Ctrl *c) {
 }
 
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(volatile const int *)p; }
+
+// Iteration cap of the build's lock retries and the sort's wait for a
+// parent, read once per thread (the Ctrl line is busy with the build's
+// allocation atomics).  The TMA waits keep kSpinCap: they must outlast their
+// own copies.
+__device__ __forceinline__ long long tree_spin_cap(const Ctrl *c) {
+    const int v = c->spin_cap;
+    return v > 0 ? (long long)v : kSpinCap;
+}
 __device__ __forceinline__ void st_volatile(int *p, int v) { *(volatile int *)p = v; }
 
 // Opening thresholds per depth, as in the oracle's orc_bh_thresholds.

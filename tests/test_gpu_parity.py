@@ -365,3 +365,33 @@ def test_tree_after_steps_equals_the_oracle(gpu, oracle):
     srt_o, _ = oracle.sort_bodies(t.children, n, t.root)
     assert np.array_equal(sim.stage_debug(nb.DEBUG_SORTED), srt_o)
     sim.close()
+
+
+def test_bounded_wait_gives_up_and_the_handle_recovers(gpu):
+    """The timeout path, exercised without a hang: with the tree stages' wait
+    cap at one iteration the sort's waits for parents give up, the step
+    returns NB_ERR_SPIN_TIMEOUT and keeps the step-start state; with the
+    default cap restored the same handle steps exactly as a fresh one."""
+    nb = gpu
+    n = 200000
+    pos = normal(n, 5, (1.0, 1.0, 0.2))
+    mass = masses(n, 5, "lognormal")
+    sim = bh_sim(nb, pos, mass, 0.5, 0.005)
+    sim.set_spin_cap(1)
+    seen_timeout = False
+    for _ in range(3):
+        before = sim.get_state()[0]
+        st = sim.step(1e-3, 1, check=False)
+        assert st in (0, nb.ERR_SPIN_TIMEOUT)
+        if st:
+            seen_timeout = True
+            np.testing.assert_array_equal(sim.get_state()[0], before)
+    assert seen_timeout
+    sim.set_spin_cap(0)
+    sim.set_state(pos, mass)
+    assert sim.step(1e-3, 2, check=False) == 0
+    fresh = bh_sim(nb, pos, mass, 0.5, 0.005)
+    fresh.step(1e-3, 2)
+    np.testing.assert_array_equal(sim.get_state()[0], fresh.get_state()[0])
+    sim.close()
+    fresh.close()
