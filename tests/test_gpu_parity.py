@@ -395,3 +395,23 @@ def test_bounded_wait_gives_up_and_the_handle_recovers(gpu):
     np.testing.assert_array_equal(sim.get_state()[0], fresh.get_state()[0])
     sim.close()
     fresh.close()
+
+
+@pytest.mark.parametrize("quad,precision", [(0, 0), (1, 1)])
+def test_repeated_runs_are_bit_identical(gpu, quad, precision):
+    """The tree build, the sort and the walk run on many threads in a
+    schedule-dependent order, but slots are summed in slot order and every
+    group walks in its own fixed order: two runs of the same steps give the
+    same bits (positions, velocities, accelerations)."""
+    nb = gpu
+    n = 100000
+    pos = normal(n, 8, (1.0, 1.0, 0.2))
+    mass = masses(n, 8, "lognormal")
+    out = []
+    for _ in range(2):
+        sim = bh_sim(nb, pos, mass, 0.5, 0.005, quad=quad, precision=precision)
+        sim.step(1e-3, 4)
+        out.append(sim.get_state()[:3])
+        sim.close()
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
