@@ -15,8 +15,11 @@ nb_set_state from pinned host arrays, nb_step, nb_get_state into pinned host
 arrays.  The accuracy gate (RMS relative force error vs an FP64 direct sum
 on 8192 sample bodies <= 1e-3) is evaluated after the timed region.
 
-The same line carries three more measurements, each with its own timed
-region (and each available alone through --mode):
+The same line carries more measurements, each with its own timed region
+(the last three also available alone through --mode):
+  bh_configs  the plain Barnes-Hut configuration (N = 262,144 unit ball,
+           monopole, FP32) and the 4M workload at theta 0.3 and 0.8, with
+           their FP64-probe accuracy;
   direct   the TMA-tiled direct sum on N = 262,144 (interactions/s against
            the FP32-pipe roofline) and the naive kernel on N = 4096;
   batched  512 systems, N log-uniform in [1024, 262144], one CUDA graph per
@@ -445,6 +448,59 @@ def run_reference(args, dist: Dist):
 
 
 # ---------------------------------------------------------------------------
+# other Barnes-Hut configurations: the plain N = 262,144 unit ball (monopole,
+# FP32: the reference's physics) and the 4M workload at theta 0.3 and 0.8
+# ---------------------------------------------------------------------------
+BALL = dict(n=262144, theta=0.5, eps=0.01, dt=1e-3, G=1.0, steps=50)
+
+
+def bh_leg(nb, dev, cfg, pos, vel, mass, dt, steps, warmup):
+    """CUDA-event time of `steps` Barnes-Hut steps, stage times, work
+    counters and the FP64-probe accuracy after the timed region."""
+    n = cfg.num_of_bodies
+    with nb.Simulation(cfg) as s:
+        s.set_state(pos, mass, vel)
+        s.set_profiling(True)
+        s.step(dt, warmup)
+        ms = s.time_steps(dt, steps)
+        stage = s.timings()
+        inter, opened, cell_inter = s.work_counters()
+        rng = np.random.default_rng(1234)
+        sample = rng.choice(n, min(n, PROBE_SAMPLES), replace=False).astype(np.int32)
+        err_max, err_rms, _ = s.force_error(sample)
+    return {"n_bodies": n, "theta": cfg.theta, "eps": cfg.epsilon, "steps": steps, "ms_per_step": ms / steps,
+            "body_updates_per_s": n * steps / (ms / 1e3),
+            "stages_ms": {k: round(stage[k], 4) for k in ("bbox", "build", "summarize", "sort", "force")},
+            "interactions_per_body": inter / steps / n, "interactions_per_s": inter / (ms / 1e3),
+            "accuracy": {"rms_rel_err": err_rms, "max_rel_err": err_max, "samples": int(len(sample)),
+                         "oracle": "FP64 direct sum on the GPU"}}
+
+
+def run_bh_configs(args, dist: Dist):
+    import nbodysimulation_gb300 as nb
+    dev = dist.local_rank
+    out = {}
+    cfg = nb.default_config(num_of_bodies=BALL["n"], algo_config=nb.BARNES_HUT, theta=BALL["theta"],
+                            epsilon=BALL["eps"], gravitational_constant=BALL["G"], numerical_method=nb.EULER,
+                            device=dev, pos_config=nb.BALL_POS, starting_volume_radius=1.0,
+                            vel_config=nb.CIRCULAR_Z_VEL, mass_config=nb.MASS_EQUAL, seed=0)
+    pos, vel, mass = nb.generate_ic(cfg)
+    leg = bh_leg(nb, dev, cfg, pos, vel, mass, BALL["dt"], BALL["steps"], args.warmup)
+    leg["workload"] = "bh_ball_n262144_theta0.5 (monopole, FP32, circular z velocities, masses 1/N)"
+    out["ball_262k"] = leg
+    pos, vel, mass = workload_ic(nb, WORKLOAD["n"], seed=dist.rank)
+    sweep = {}
+    for theta in (0.3, 0.8):
+        c = nb.default_config(num_of_bodies=WORKLOAD["n"], algo_config=nb.BARNES_HUT, theta=theta,
+                              epsilon=WORKLOAD["eps"], gravitational_constant=WORKLOAD["G"],
+                              numerical_method=nb.EULER, device=dev, precision=nb.PRECISION_COMPENSATED,
+                              multipole=nb.MULTIPOLE_QUADRUPOLE)
+        sweep[f"theta_{theta}"] = bh_leg(nb, dev, c, pos, vel, mass, WORKLOAD["dt"], 5, args.warmup)
+    out["theta_sweep_4m"] = sweep
+    return out if dist.rank == 0 else None
+
+
+# ---------------------------------------------------------------------------
 # direct sum: tiled all-pairs on N = 262,144 and the naive kernel on N = 4096
 # ---------------------------------------------------------------------------
 DIRECT = dict(n=262144, n_global=4096, eps=0.01, eps_global=0.05, dt=1e-3, G=1.0, steps=50)
@@ -841,7 +897,8 @@ def main():
                 # the other measurements of the workload family, each its own
                 # timed region (see their modes): direct sum, batched systems
                 # against plain solves, the job server against plain solves
-                extra = {"direct": run_direct(args, dist), "batched": run_batch(args, dist)}
+                extra = {"bh_configs": run_bh_configs(args, dist), "direct": run_direct(args, dist),
+                         "batched": run_batch(args, dist)}
                 if args.serve_seconds is None:
                     args.serve_seconds = SERVE["seconds_in_step"]
                 extra["serving"] = run_serve(args, dist)

@@ -62,6 +62,7 @@ def rel_to_typical(a, b):
 
 
 CASES = [
+    ("ball", 262144, 0.5, 0.01, 0, 0),  # the plain Barnes-Hut configuration's size
     ("ball", 20000, 0.5, 0.01, 0, 0),
     ("normal", 30000, 0.5, 0.005, 0, 0),
     ("normal", 12345, 0.3, 0.005, 0, 0),
