@@ -92,6 +92,7 @@ __device__ __forceinline__ int insert_body(const DevSim &s, const Geo &root_g, i
     int *cslot = &s.child[(node - n) * 8 + slot];
     int ch = ld_volatile(cslot);
     long long spins = 0;
+    unsigned pause = 32;
     while (true) {
         while (ch >= n) {  // descend through published cells
             node = ch;
@@ -153,6 +154,10 @@ __device__ __forceinline__ int insert_body(const DevSim &s, const Geo &root_g, i
             return -1;
         }
         if ((spins & 1023) == 0 && read_status(ctrl)) return -1;
+        if (ch == kLocked) {  // another thread is splitting this slot: back off
+            __nanosleep(pause);
+            if (pause < 2048) pause <<= 1;
+        }
         ch = ld_volatile(cslot);
     }
 }
