@@ -396,7 +396,9 @@ nb_status nb_server_job_info(nb_server *s, int64_t job, nb_job_info *out);
  * NB_ERR_SPIN_TIMEOUT after timeout_s seconds (< 0: no limit). */
 nb_status nb_server_wait(nb_server *s, int64_t job, double timeout_s);
 /* Final state of a finished job when the server has no callback (copied
- * once, then released); either array may be NULL. */
+ * once, then released); either array may be NULL.  Without a callback the
+ * results stay in host memory until fetched; every job keeps a small record
+ * (its config and times, for nb_server_job_info) until nb_server_destroy. */
 nb_status nb_server_result(nb_server *s, int64_t job, float *pos3, float *vel3);
 typedef struct nb_server_stats {
     int64_t submitted, completed, failed, queued, running;

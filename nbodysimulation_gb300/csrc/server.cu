@@ -347,6 +347,9 @@ static void schedule_loop(nb_server *s) {
         cudaError_t e = cudaSuccess;
         for (auto &j : fresh) {
             if (e == cudaSuccess) e = cudaStreamWaitEvent(s->compute, j->uploaded, 0);
+            // the wait is enqueued; the event is released once it has completed
+            cudaEventDestroy(j->uploaded);
+            j->uploaded = nullptr;
             run.push_back(j);
         }
         std::vector<int> remaining;
