@@ -416,3 +416,24 @@ def test_repeated_runs_are_bit_identical(gpu, quad, precision):
         sim.close()
     for a, b in zip(*out):
         np.testing.assert_array_equal(a, b)
+
+
+def test_largest_tree_and_the_size_limit(gpu):
+    """The walk packs (level << 26) | node, so N + cells + 1 < 2^26: N = 2^24
+    steps normally (with the default 2N cells), and a size past the limit is
+    refused at creation with NB_ERR_UNSUPPORTED."""
+    nb = gpu
+    n = 1 << 24
+    rng = np.random.default_rng(1)
+    pos = rng.normal(size=(n, 3)).astype(np.float32)
+    mass = np.full(n, 1.0 / n, np.float32)
+    sim = bh_sim(nb, pos, mass, 0.7, 0.01)
+    sim.step(1e-3, 1)
+    p = sim.get_state()[0]
+    assert np.all(np.isfinite(p))
+    info = sim.stage_debug(nb.DEBUG_TREE_INFO)
+    assert int(info[1]) == 2 * n  # cell capacity
+    sim.close()
+    with pytest.raises(nb.NbError) as e:
+        nb.Simulation(num_of_bodies=23_000_000, algo_config=nb.BARNES_HUT)
+    assert e.value.status == nb.ERR_UNSUPPORTED
