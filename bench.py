@@ -708,7 +708,7 @@ def run_batch(args, dist: Dist):
 # ---------------------------------------------------------------------------
 SERVE = dict(name="serve_poisson200_n1k_1m", rate=200.0, seconds=2.0, n_min=1024, n_max=1048576, steps_min=10,
              steps_max=500, thetas=(0.5, 0.7), eps=0.01, dt=1e-3, G=1.0, direct_below=8192, budget=120e9,
-             snapshot_every=10, seed=0, seconds_in_step=0.5)
+             snapshot_every=10, seed=0, seconds_in_step=1.0)
 
 
 def serve_jobs(nb, rate, seconds, seed):
@@ -796,7 +796,9 @@ def run_plain_arm(nb, jobs, dt, dev):
                 k = min(SERVE["snapshot_every"], steps - done)
                 s.step(dt, k)
                 done += k
-                s.get_state()
+                # the served path returns the same: positions at every
+                # snapshot, positions and velocities at the end
+                s.positions(with_velocities=done == steps)
         lat.append(time.perf_counter() - t0 - t)
         total += cfg.num_of_bodies * steps
     span = time.perf_counter() - t0 - jobs[0][0]

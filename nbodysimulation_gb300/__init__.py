@@ -243,6 +243,15 @@ class Simulation:
                                         mass.ctypes.data), "nb_get_state")
         return pos, vel, acc, mass
 
+    def positions(self, with_velocities=False):
+        """Positions (N,3) -- what a snapshot or a renderer reads -- and, when
+        asked, velocities."""
+        pos = np.zeros((self.n, 3), np.float32)
+        vel = np.zeros((self.n, 3), np.float32) if with_velocities else None
+        self._check(self.L.nb_get_state(self.h, pos.ctypes.data, None if vel is None else vel.ctypes.data, None,
+                                        None), "nb_get_state")
+        return (pos, vel) if with_velocities else pos
+
     def step(self, dt, nsteps=1, check=True):
         st = self.L.nb_step(self.h, dt, nsteps)
         if check:

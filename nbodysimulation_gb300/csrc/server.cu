@@ -65,7 +65,7 @@ struct Delivery {
     JobP job;
     int final_state = 0;  // 0 snapshot, 1 final
     int step = 0;
-    char *dbuf = nullptr;  // body float4[n] (+ vel float4[n]) + Ctrl
+    char *dbuf = nullptr;  // positions float[3n] (+ velocities float[3n]) + Ctrl
     size_t bytes = 0;
     cudaEvent_t ready = nullptr;
 };
@@ -140,35 +140,55 @@ static int64_t job_bytes(nb_server *s, Job &j) {
     return (int64_t)(sysmem_layout(m, nullptr) + kCtrlBytes);
 }
 
-static cudaError_t upload_job(nb_server *s, Job &j) {
+// Packs the job's state into pinned staging ({x,y,z,m} and {vx,vy,vz,0}
+// float4 arrays, then its Ctrl) and uploads it on the upload stream.
+static cudaError_t upload_job(nb_server *s, Job &j, char *&stage, size_t &stage_cap) {
     cudaError_t e = cudaMallocAsync((void **)&j.dmem, (size_t)j.bytes, s->upload);
     if (e != cudaSuccess) return e;
     sysmem_layout(j.mem, j.dmem);
     j.mem.ctrl = reinterpret_cast<Ctrl *>(j.dmem + (size_t)j.bytes - kCtrlBytes);
     const size_t n = (size_t)j.n;
-    std::vector<float4> body(n), vel(n);
+    const size_t need = 32 * n + sizeof(Ctrl);
+    if (need > stage_cap) {
+        if (stage) cudaFreeHost(stage);
+        stage_cap = need + need / 4;
+        if ((e = cudaMallocHost((void **)&stage, stage_cap)) != cudaSuccess) {
+            stage = nullptr;
+            stage_cap = 0;
+            return e;
+        }
+    }
+    float4 *body = reinterpret_cast<float4 *>(stage), *vel = body + n;
     for (size_t i = 0; i < n; ++i) {
         body[i] = make_float4(j.pos[3 * i], j.pos[3 * i + 1], j.pos[3 * i + 2], j.mass[i]);
         vel[i] = j.vel.empty() ? make_float4(0.f, 0.f, 0.f, 0.f)
                                : make_float4(j.vel[3 * i], j.vel[3 * i + 1], j.vel[3 * i + 2], 0.0f);
     }
-    Ctrl init{};
-    init.budget = j.steps;
-    // pageable sources: each call returns once its source has been consumed
-    if ((e = cudaMemcpyAsync(j.mem.body[0], body.data(), 16 * n, cudaMemcpyHostToDevice, s->upload)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(j.mem.vel, vel.data(), 16 * n, cudaMemcpyHostToDevice, s->upload)) != cudaSuccess ||
+    Ctrl *init = reinterpret_cast<Ctrl *>(vel + n);
+    memset(init, 0, sizeof(Ctrl));
+    init->budget = j.steps;
+    if ((e = cudaMemcpyAsync(j.mem.body[0], body, 16 * n, cudaMemcpyHostToDevice, s->upload)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(j.mem.vel, vel, 16 * n, cudaMemcpyHostToDevice, s->upload)) != cudaSuccess ||
         (e = cudaMemsetAsync(j.mem.acc, 0, 16 * n, s->upload)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(j.mem.ctrl, &init, sizeof(Ctrl), cudaMemcpyHostToDevice, s->upload)) != cudaSuccess)
+        (e = cudaMemcpyAsync(j.mem.ctrl, init, sizeof(Ctrl), cudaMemcpyHostToDevice, s->upload)) != cudaSuccess)
         return e;
     if ((e = cudaEventCreateWithFlags(&j.uploaded, cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(j.uploaded, s->upload)) != cudaSuccess) return e;
     j.desc = sysmem_desc(j.mem, j.cfg, j.dt);
-    // the copies above were issued from pageable memory and have been staged
+    // the staging is reused by the next job
     return cudaStreamSynchronize(s->upload);
 }
 
 static void admit_loop(nb_server *s) {
     cudaSetDevice(s->dev);
+    char *stage = nullptr;  // pinned upload staging, grown to the largest job
+    size_t stage_cap = 0;
+    struct FreeStage {
+        char *&p;
+        ~FreeStage() {
+            if (p) cudaFreeHost(p);
+        }
+    } free_stage{stage};
     while (true) {
         JobP j;
         {
@@ -202,7 +222,7 @@ static void admit_loop(nb_server *s) {
             s->adm.reserve(j->bytes);
             s->queue.pop_front();
         }
-        cudaError_t e = upload_job(s, *j);
+        cudaError_t e = upload_job(s, *j, stage, stage_cap);
         j->pos = std::vector<float>();
         j->vel = std::vector<float>();
         j->mass = std::vector<float>();
@@ -228,23 +248,30 @@ static void admit_loop(nb_server *s) {
 // ---------------------------------------------------------------------------
 // Copies the current body buffer (+ velocities when final) and the status
 // word of job j to a new device buffer, in stream order after the round.
+// Unpacks the current positions (+ velocities when final) of job j into a
+// new device buffer in the reference's float[3N] layout, and copies its
+// status word after them, in stream order after the round.
+static size_t copy_out_ctrl_offset(int n, bool final_state) {
+    const size_t b = (final_state ? 24 : 12) * (size_t)n;
+    return (b + 15) & ~(size_t)15;
+}
+
 static cudaError_t enqueue_copy_out(nb_server *s, const JobP &j, bool final_state, std::deque<Delivery> &out) {
     Delivery d;
     d.job = j;
     d.final_state = final_state ? 1 : 0;
     d.step = j->done;
-    const size_t nb = 16 * (size_t)j->n;
-    d.bytes = (final_state ? 2 * nb : nb) + sizeof(Ctrl);
+    const size_t n = (size_t)j->n;
+    const size_t off = copy_out_ctrl_offset(j->n, final_state);
+    d.bytes = off + sizeof(Ctrl);
     cudaError_t e = cudaMallocAsync((void **)&d.dbuf, d.bytes, s->compute);
     if (e != cudaSuccess) return e;
     const float4 *cur = j->mem.body[j->done & 1];  // every step flips the current buffer
-    if ((e = cudaMemcpyAsync(d.dbuf, cur, nb, cudaMemcpyDeviceToDevice, s->compute)) != cudaSuccess) return e;
-    size_t off = nb;
-    if (final_state) {
-        if ((e = cudaMemcpyAsync(d.dbuf + off, j->mem.vel, nb, cudaMemcpyDeviceToDevice, s->compute)) != cudaSuccess)
-            return e;
-        off += nb;
-    }
+    float *pos3 = reinterpret_cast<float *>(d.dbuf);
+    float *vel3 = final_state ? pos3 + 3 * n : nullptr;
+    if ((e = launch_unpack(cur, final_state ? j->mem.vel : nullptr, nullptr, pos3, vel3, nullptr, j->n,
+                           s->compute)) != cudaSuccess)
+        return e;
     if ((e = cudaMemcpyAsync(d.dbuf + off, j->mem.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToDevice, s->compute)) !=
         cudaSuccess)
         return e;
@@ -402,44 +429,42 @@ static void schedule_loop(nb_server *s) {
 // ---------------------------------------------------------------------------
 static void deliver_loop(nb_server *s) {
     cudaSetDevice(s->dev);
-    std::vector<float4> hb;
-    std::vector<float> pos, vel;
+    char *pinned = nullptr;  // host staging, grown to the largest delivery
+    size_t pinned_cap = 0;
     while (true) {
         Delivery d;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv_deliver.wait(lk, [&] { return s->deliver_stop || !s->deliveries.empty(); });
-            if (s->deliveries.empty()) return;
+            if (s->deliveries.empty()) break;
             d = s->deliveries.front();
             s->deliveries.pop_front();
         }
         const int n = d.job->n;
-        cudaError_t e = cudaStreamWaitEvent(s->out, d.ready, 0);
-        hb.resize(d.bytes / 16 + 1);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(hb.data(), d.dbuf, d.bytes, cudaMemcpyDeviceToHost, s->out);
+        cudaError_t e = cudaSuccess;
+        if (d.bytes > pinned_cap) {
+            if (pinned) cudaFreeHost(pinned);
+            pinned_cap = d.bytes + d.bytes / 4;
+            e = cudaMallocHost((void **)&pinned, pinned_cap);
+            if (e != cudaSuccess) {
+                pinned = nullptr;
+                pinned_cap = 0;
+            }
+        }
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->out, d.ready, 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(pinned, d.dbuf, d.bytes, cudaMemcpyDeviceToHost, s->out);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->out);
         cudaFreeAsync(d.dbuf, s->out);
         cudaEventDestroy(d.ready);
         Ctrl c{};
-        const size_t nb = 16 * (size_t)n;
-        memcpy(&c, reinterpret_cast<const char *>(hb.data()) + (d.final_state ? 2 * nb : nb), sizeof(Ctrl));
+        if (e == cudaSuccess) memcpy(&c, pinned + copy_out_ctrl_offset(n, d.final_state != 0), sizeof(Ctrl));
         const int status = e != cudaSuccess ? NB_ERR_CUDA : c.status;
-        pos.resize(3 * (size_t)n);
-        for (int i = 0; i < n; ++i) {
-            pos[3 * (size_t)i] = hb[i].x;
-            pos[3 * (size_t)i + 1] = hb[i].y;
-            pos[3 * (size_t)i + 2] = hb[i].z;
-        }
+        const float *pos = reinterpret_cast<const float *>(pinned);
+        const float *vel = pos + 3 * (size_t)n;
         const JobP &j = d.job;
         if (!d.final_state) {
-            if (s->fn && status == 0) s->fn(s->user, j->id, NB_JOB_EVENT_SNAPSHOT, d.step, pos.data(), nullptr, n);
+            if (s->fn && status == 0) s->fn(s->user, j->id, NB_JOB_EVENT_SNAPSHOT, d.step, pos, nullptr, n);
             continue;
-        }
-        vel.resize(3 * (size_t)n);
-        for (int i = 0; i < n; ++i) {
-            vel[3 * (size_t)i] = hb[n + i].x;
-            vel[3 * (size_t)i + 1] = hb[n + i].y;
-            vel[3 * (size_t)i + 2] = hb[n + i].z;
         }
         {
             std::lock_guard<std::mutex> g(s->mu);
@@ -455,19 +480,20 @@ static void deliver_loop(nb_server *s) {
                 s->latencies.push_back(j->t_done - j->t_submit);
                 s->last_done = std::max(s->last_done, j->t_done);
                 if (!s->fn) {
-                    j->res_pos = pos;
-                    j->res_vel = vel;
+                    j->res_pos.assign(pos, pos + 3 * (size_t)n);
+                    j->res_vel.assign(vel, vel + 3 * (size_t)n);
                     j->have_result = true;
                 }
             }
         }
         if (s->fn) {
             if (status) s->fn(s->user, j->id, NB_JOB_EVENT_FAILED, status, nullptr, nullptr, n);
-            else s->fn(s->user, j->id, NB_JOB_EVENT_DONE, j->steps, pos.data(), vel.data(), n);
+            else s->fn(s->user, j->id, NB_JOB_EVENT_DONE, j->steps, pos, vel, n);
         }
         std::lock_guard<std::mutex> g(s->mu);
         s->cv_done.notify_all();
     }
+    if (pinned) cudaFreeHost(pinned);
 }
 
 // ---------------------------------------------------------------------------
