@@ -232,3 +232,19 @@ def test_cpp_host_mirror_on_gpu(gpu, tmp_path):
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     assert r.stdout.startswith("stepped 1024"), r.stdout
     assert "batched 2 1024" in r.stdout and "served 0 1" in r.stdout, r.stdout
+
+
+@pytest.mark.skipif(__import__("platform").machine() != "x86_64", reason="pins this host's libm results")
+def test_ic_generator_bytes_are_pinned(nbgb_lib):
+    """The generator runs in parallel chunks whose streams are jumped to their
+    first draw; its bytes must stay those of one sequential pass (hashes taken
+    from the sequential generator, N = 70001 so the chunks are uneven)."""
+    import hashlib
+    nb = nbgb_lib
+    want = {(2, 5, 1): "e47e1189cfd02c74", (3, 0, 2): "ebe7a3499cf0ebf6", (1, 3, 0): "8f92c617a6525aec",
+            (0, 4, 0): "0b6961088e10c8c5"}
+    for (pc, vc, mc), h in want.items():
+        c = nb.default_config(num_of_bodies=70001, pos_config=pc, vel_config=vc, mass_config=mc, seed=11,
+                              starting_volume_radius=1.0, gravitational_constant=1.0)
+        p, v, m = nb.generate_ic(c)
+        assert hashlib.sha256(p.tobytes() + v.tobytes() + m.tobytes()).hexdigest()[:16] == h, (pc, vc, mc)
