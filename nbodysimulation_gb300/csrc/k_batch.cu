@@ -14,7 +14,6 @@
 
 namespace nbgb {
 
-constexpr int kChunk = kBatchChunk;
 
 // ---------------------------------------------------------------------------
 // reset (init, kernels/init.cl:26-33) for every Barnes-Hut system
@@ -49,8 +48,8 @@ __global__ void __launch_bounds__(256) k_batch_bbox(BatchTables t) {
     const SysDesc &d = t.sys[k];
     if (!system_live(d.v.ctrl)) return;  // block-uniform
     const DevSim s = system_view(d);
-    const int i0 = (blockIdx.x - d.chunk_begin) * kChunk;
-    const int i1 = min(s.n, i0 + kChunk);
+    const int i0 = (blockIdx.x - d.chunk_begin) * d.chunk;
+    const int i1 = min(s.n, i0 + d.chunk);
     unsigned mn0 = 0xFFFFFFFFu, mn1 = 0xFFFFFFFFu, mn2 = 0xFFFFFFFFu, mx0 = 0u, mx1 = 0u, mx2 = 0u;
     int bad = -1;
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
@@ -109,8 +108,8 @@ __global__ void __launch_bounds__(256) k_batch_build(BatchTables t) {
     const SysDesc &d = t.sys[k];
     const DevSim s = system_view(d);
     if (read_status(s.ctrl) || !system_live(s.ctrl)) return;
-    const int i0 = (blockIdx.x - d.chunk_begin) * kChunk;
-    const int i1 = min(s.n, i0 + kChunk);
+    const int i0 = (blockIdx.x - d.chunk_begin) * d.chunk;
+    const int i1 = min(s.n, i0 + d.chunk);
     const int depth = d.p.tree_ref ? build_chunk<RefBox, true>(s, i0, i1) : build_chunk<GeoCube, false>(s, i0, i1);
     if (depth < 0) return;
     const unsigned am = __activemask();
@@ -214,10 +213,15 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
     __shared__ float4 s_cpm[kForceWarps][32];
     __shared__ float4 s_cmeta[kForceWarps][32];
     __shared__ float4 s_cqa[kForceWarps][kQuad ? 32 : 1];
+    // the current system's buffers and parameters, one copy per warp: the
+    // walk reads them from shared memory where the single-system kernel reads
+    // its kernel parameters, instead of holding them in registers
+    __shared__ DevSim s_view[kForceWarps];
+    __shared__ StepParams s_par[kForceWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const WarpStage ws{s_stack[w], s_bpm[w], s_cpm[w], s_cmeta[w], s_cqa[w]};
     float *dq = s_dq[w];
-    int cur = -1;
+    int cur = -1, begin = 0;
     int mode = 0;  // 0 walk, 1 keep the step-start state (failed step), 2 inert
     while (true) {
         int gg = 0;
@@ -225,40 +229,43 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
         gg = __shfl_sync(0xffffffffu, gg, 0);
         if (gg >= t.groups) break;
         const int k = find_system(t.group_prefix, t.nsys, gg);
-        const SysDesc &d = t.sys[k];
-        const DevSim s = system_view(d);
-        StepParams p = d.p;
-        p.kdk_primed = s.ctrl->kdk_primed;
         if (k != cur) {
             cur = k;
+            __syncwarp();  // the previous system's view and thresholds are no longer read
             int sk = 0;
             if (lane == 0) {
-                if (!system_live(s.ctrl)) {
+                const SysDesc &d = t.sys[k];
+                const DevSim v = system_view(d);
+                StepParams p = d.p;
+                p.kdk_primed = v.ctrl->kdk_primed;
+                s_view[w] = v;
+                s_par[w] = p;
+                if (!system_live(v.ctrl)) {
                     sk = 2;
-                } else if (read_status(s.ctrl)) {
+                } else if (read_status(v.ctrl)) {
                     sk = 1;
-                } else if (s.ctrl->max_depth >= kMaxDepth) {
-                    set_status(s.ctrl, kStDepth, s.ctrl->max_depth);
+                } else if (v.ctrl->max_depth >= kMaxDepth) {
+                    set_status(v.ctrl, kStDepth, v.ctrl->max_depth);
                     sk = 1;
                 }
+                float box[6];
+                load_box(v.ctrl, box);
+                make_thresholds(box, p.theta, p.eps, p.crit_ref, dq);
+                begin = d.group_begin;
             }
             mode = __shfl_sync(0xffffffffu, sk, 0);
-            __syncwarp();  // the previous system's thresholds are no longer read
-            if (lane == 0) {
-                float box[6];
-                load_box(s.ctrl, box);
-                make_thresholds(box, p.theta, p.eps, p.crit_ref, dq);
-            }
+            begin = __shfl_sync(0xffffffffu, begin, 0);
             __syncwarp();
         }
-        const int g = gg - d.group_begin;
+        const int g = gg - begin;
+        const DevSim &s = s_view[w];
         if (mode == 2) continue;
         if (mode == 1) {  // keep the step-start state
             const int i = g * 32 + lane;
             if (i < s.n) s.body_next[i] = s.body_cur[i];
             continue;
         }
-        force_group<kMethod, kComp, false, kQuad>(s, p, dq, g, lane, ws);
+        force_group<kMethod, kComp, false, kQuad>(s, s_par[w], dq, g, lane, ws);
     }
 }
 

@@ -162,6 +162,7 @@ struct SysDesc {
     int cell_begin;    // prefix over BH systems' cell slots (cap + 1)
     int group_begin;   // prefix over BH systems' warp groups
     int dblock_begin;  // prefix over direct systems' target blocks
+    int chunk;         // bodies per bbox / build block (batch_chunk)
 };
 
 // Prefix tables (nsys + 1 entries each) and totals of a batch.
@@ -223,7 +224,16 @@ cudaError_t launch_diagnostics(const float4 *body, const float4 *vel, int n, int
                                double G, double *out9, cudaStream_t st);
 
 // batched systems (k_batch.cu)
-constexpr int kBatchChunk = 4096;  // bodies per bbox / build block
+// Bodies per bbox / build block of a batched tree.  Threads that start at a
+// root together contend for its first cells, so fewer per tree is better
+// once the batch as a whole has threads enough: 4096 when the batch's trees
+// hold 4M bodies or more, or for a tree of 2^19 bodies or more; 1024
+// otherwise (measured: a 512-system batch of 27M bodies builds in 3.6 ms
+// with 4096 and 6.6 ms with 1024; a lone 131k-body tree steps in 0.67 ms
+// with 1024 and 0.81 ms with 4096).
+inline int batch_chunk(int n, long long batch_tree_bodies) {
+    return (n >= (1 << 19) || batch_tree_bodies >= (4LL << 20)) ? 4096 : 1024;
+}
 int batch_direct_variants();
 int batch_direct_block_bodies(int variant);
 cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int quad, int direct_variant,

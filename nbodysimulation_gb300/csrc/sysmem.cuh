@@ -126,6 +126,9 @@ inline SysDesc sysmem_desc(const SysMem &m, const nb_config &c, float dt) {
 inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, int totals[4]) {
     int *chunk = pref, *cell = pref + (nsys + 1), *group = pref + 2 * (nsys + 1), *dblock = pref + 3 * (nsys + 1);
     chunk[0] = cell[0] = group[0] = dblock[0] = 0;
+    long long tree_bodies = 0;
+    for (int k = 0; k < nsys; ++k)
+        if (sys[k].active && sys[k].kind == kSysBH) tree_bodies += sys[k].v.n;
     int body = 0;
     for (int k = 0; k < nsys; ++k) {
         SysDesc &d = sys[k];
@@ -136,7 +139,8 @@ inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, 
         d.group_begin = group[k];
         d.dblock_begin = dblock[k];
         const bool bh = d.active && d.kind == kSysBH, direct = d.active && d.kind == kSysDirect;
-        chunk[k + 1] = chunk[k] + (bh ? (n + kBatchChunk - 1) / kBatchChunk : 0);
+        d.chunk = batch_chunk(n, tree_bodies);
+        chunk[k + 1] = chunk[k] + (bh ? (n + d.chunk - 1) / d.chunk : 0);
         cell[k + 1] = cell[k] + (bh ? d.v.cap + 1 : 0);
         group[k + 1] = group[k] + (bh ? (n + 31) / 32 : 0);
         dblock[k + 1] = dblock[k] + (direct ? (n + direct_block - 1) / direct_block : 0);
