@@ -172,11 +172,16 @@ __global__ void __launch_bounds__(kScanThreads) k_batch_used(BatchTables t) {
 __global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
     const int total = t.used_prefix[t.nsys];
     const int stride = gridDim.x * blockDim.x;
+    int k = 0, lo = 0, hi = 0;  // the system of the last x and its range (x only grows)
     for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
-        const int k = find_system(t.used_prefix, t.nsys, x);
+        if (x >= hi) {
+            k = find_system(t.used_prefix, t.nsys, x);
+            lo = t.used_prefix[k];
+            hi = t.used_prefix[k + 1];
+        }
         const SysDesc &d = t.sys[k];
         const DevSim s = system_view(d);
-        const int node = s.ctrl->bottom + (x - t.used_prefix[k]);
+        const int node = s.ctrl->bottom + (x - lo);
         if (d.p.quadrupole) summarize_from<true>(s, node);
         else summarize_from<false>(s, node);
     }
@@ -191,12 +196,17 @@ __global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
 __global__ void __launch_bounds__(256) k_batch_sort(BatchTables t) {
     const int total = t.used_prefix[t.nsys];
     const int stride = gridDim.x * blockDim.x;
+    int k = 0, lo = 0, hi = 0;  // the system of the last x and its range (x only grows)
     for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
-        const int k = find_system(t.used_prefix, t.nsys, x);
+        if (x >= hi) {
+            k = find_system(t.used_prefix, t.nsys, x);
+            lo = t.used_prefix[k];
+            hi = t.used_prefix[k + 1];
+        }
         const SysDesc &d = t.sys[k];
         const DevSim s = system_view(d);
         if (read_status(s.ctrl)) continue;
-        sort_cell(s, s.n + s.cap - (x - t.used_prefix[k]), tree_spin_cap(s.ctrl));
+        sort_cell(s, s.n + s.cap - (x - lo), tree_spin_cap(s.ctrl));
     }
 }
 
