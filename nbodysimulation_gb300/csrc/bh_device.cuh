@@ -209,12 +209,20 @@ __device__ __forceinline__ void summarize_from(const DevSim &s, int k) {
         const int c = node - n;
         float M = 0.0f, cx = 0.0f, cy = 0.0f, cz = 0.0f;
         int cnt = 0, w = 0;
-        int wc[8];
-        float4 wp[8];
+        // children in slot order; the compacted list and packed lines go to
+        // the cell's rows.  The monopole kernel stores them as they come
+        // (fewer registers, more warps); the quadrupole pass needs them again,
+        // so that kernel gathers them in registers and stores whole rows.
+        int wc[kQuad ? 8 : 1];
+        float4 wp[kQuad ? 8 : 1];
+        int *wrow = &s.wchild[c * 8];
+        float4 *prow = &s.wpm[c * 8];
+        if constexpr (kQuad) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            wc[j] = kEmpty;
-            wp[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            for (int j = 0; j < 8; ++j) {
+                wc[j] = kEmpty;
+                wp[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -234,18 +242,29 @@ __device__ __forceinline__ void summarize_from(const DevSim &s, int k) {
             cy = __fadd_rn(cy, __fmul_rn(pm.y, pm.w));
             cz = __fadd_rn(cz, __fmul_rn(pm.z, pm.w));
             cnt += cc;
-            // w <= j, so a static index write through a select chain
+            if constexpr (kQuad) {
+                // w <= j, so a static index write through a select chain
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (q == w) { wc[q] = ch; wp[q] = pm; }
+                for (int q = 0; q < 8; ++q)
+                    if (q == w) { wc[q] = ch; wp[q] = pm; }
+            } else {
+                wrow[w] = ch;
+                prow[w] = pm;
+            }
             ++w;
         }
-        int4 *wrow = reinterpret_cast<int4 *>(&s.wchild[c * 8]);
-        wrow[0] = make_int4(wc[0], wc[1], wc[2], wc[3]);
-        wrow[1] = make_int4(wc[4], wc[5], wc[6], wc[7]);
-        float4 *prow = &s.wpm[c * 8];
+        if constexpr (kQuad) {
+            int4 *r4 = reinterpret_cast<int4 *>(wrow);
+            r4[0] = make_int4(wc[0], wc[1], wc[2], wc[3]);
+            r4[1] = make_int4(wc[4], wc[5], wc[6], wc[7]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) prow[q] = wp[q];
+            for (int q = 0; q < 8; ++q) prow[q] = wp[q];
+        } else {
+            for (int q = w; q < 8; ++q) {
+                wrow[q] = kEmpty;
+                prow[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+        }
         const float inv = __frcp_rn(M);
         const float X = __fmul_rn(cx, inv), Y = __fmul_rn(cy, inv), Z = __fmul_rn(cz, inv);
         s.count[c] = cnt;

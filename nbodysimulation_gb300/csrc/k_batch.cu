@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(kScanThreads) k_batch_used(BatchTables t) {
 // ---------------------------------------------------------------------------
 // summarize: one allocated cell per thread over all trees
 // ---------------------------------------------------------------------------
+template <bool kQuad>
 __global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
     const int total = t.used_prefix[t.nsys];
     const int stride = gridDim.x * blockDim.x;
@@ -181,9 +182,7 @@ __global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
         }
         const SysDesc &d = t.sys[k];
         const DevSim s = system_view(d);
-        const int node = s.ctrl->bottom + (x - lo);
-        if (d.p.quadrupole) summarize_from<true>(s, node);
-        else summarize_from<false>(s, node);
+        summarize_from<kQuad>(s, s.ctrl->bottom + (x - lo));
     }
 }
 
@@ -460,7 +459,8 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
         int sblocks = sm_count * 8;
         const int need = (t.cells + 255) / 256;
         if (sblocks > need) sblocks = need;
-        k_batch_summarize<<<sblocks, 256, 0, st>>>(t);
+        if (quad) k_batch_summarize<true><<<sblocks, 256, 0, st>>>(t);
+        else k_batch_summarize<false><<<sblocks, 256, 0, st>>>(t);
         int rblocks = resident((const void *)k_batch_sort, 256, sm_count);
         if (rblocks > need) rblocks = need;
         k_batch_sort<<<rblocks, 256, 0, st>>>(t);
