@@ -170,6 +170,7 @@ nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out) {
     b->mem.resize(nsys);
     size_t total = 0;
     int maxn = 0;
+    long long bodies_total = 0, cells_total = 0;
     for (int k = 0; k < nsys; ++k) {
         const nb_config &c = cfgs[k];
         SysMem &m = b->mem[k];
@@ -180,6 +181,10 @@ nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out) {
         if (m.tree && (long long)m.n + m.cap + 1 >= (1LL << 26) - 1) return fail_all(NB_ERR_UNSUPPORTED);
         total = sysmem_align(total) + sysmem_layout(m, nullptr);
         maxn = std::max(maxn, m.n);
+        // the batch-wide index spaces (bodies, cell slots) are 32-bit
+        bodies_total += m.n;
+        cells_total += m.tree ? (long long)m.cap + 1 : 0;
+        if (bodies_total >= (1LL << 31) - 1 || cells_total >= (1LL << 31) - 1) return fail_all(NB_ERR_UNSUPPORTED);
     }
     if (cudaMalloc(&b->arena, total) != cudaSuccess) return fail_all(NB_ERR_OUT_OF_MEMORY);
     size_t off = 0;
