@@ -437,3 +437,21 @@ def test_largest_tree_and_the_size_limit(gpu):
     with pytest.raises(nb.NbError) as e:
         nb.Simulation(num_of_bodies=23_000_000, algo_config=nb.BARNES_HUT)
     assert e.value.status == nb.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("eps", [0.01, 0.0])
+def test_theta_zero_opens_every_cell(gpu, oracle, eps):
+    """theta = 0 accepts no cell, so the walk reaches every body: the
+    accelerations equal the FP64 direct sum to FP32 rounding (with eps = 0
+    the self pair is skipped)."""
+    nb = gpu
+    n = 4000
+    pos = ball(n, 21)
+    mass = masses(n, 21, "lognormal")
+    sim = bh_sim(nb, pos, mass, 0.0, eps)
+    sim.step(0.0, 1)
+    acc = sim.get_state()[2]
+    sim.close()
+    ref = oracle.direct_fp64(pos, mass, eps, 1.0)
+    rel = np.linalg.norm(acc - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert np.sqrt(np.mean(rel ** 2)) < 2e-5 and np.max(rel) < 2e-3
