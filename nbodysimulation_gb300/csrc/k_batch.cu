@@ -14,7 +14,6 @@
 
 namespace nbgb {
 
-
 // ---------------------------------------------------------------------------
 // reset (init, kernels/init.cl:26-33) for every Barnes-Hut system
 // ---------------------------------------------------------------------------
