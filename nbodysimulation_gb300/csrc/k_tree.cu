@@ -6,6 +6,8 @@
 // saturate_tree (kernels/saturate_tree.cl) and the empty sort
 // (kernels/sort.cl).  Each is re-designed for sm_103a; the differences that
 // change results are listed at each kernel.
+#include <algorithm>
+
 #include "bh_device.cuh"
 
 namespace nbgb {
@@ -157,7 +159,11 @@ cudaError_t launch_bbox(const DevSim &s, int sm_count, cudaStream_t st) {
 
 cudaError_t launch_build(const DevSim &s, int tree_ref, int sm_count, cudaStream_t st) {
     const void *fn = tree_ref ? (const void *)k_build<RefBox, true> : (const void *)k_build<GeoCube, false>;
-    int blocks = resident_blocks(fn, 256, sm_count);
+    // two blocks per SM: threads that start at the root together contend for
+    // its first cells, and fewer of them insert faster (measured build time
+    // with 1 / 2 / 4 / 8 blocks per SM: 262k-body ball 0.20 / 0.20 / 0.30 /
+    // 0.32 ms, 1M 0.60 / 0.41 / 0.49 / 0.54 ms, 4M 2.25 / 1.26 / 1.24 / 1.32 ms)
+    int blocks = std::min(resident_blocks(fn, 256, sm_count), 2 * sm_count);
     const int need = (s.n + 255) / 256;
     if (blocks > need) blocks = need > 0 ? need : 1;
     if (tree_ref) k_build<RefBox, true><<<blocks, 256, 0, st>>>(s);
