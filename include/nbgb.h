@@ -371,7 +371,10 @@ enum { NB_JOB_QUEUED = 0, NB_JOB_RUNNING = 1, NB_JOB_DONE = 2, NB_JOB_FAILED = 3
 enum { NB_JOB_EVENT_SNAPSHOT = 0, NB_JOB_EVENT_DONE = 1, NB_JOB_EVENT_FAILED = 2 };
 /* event SNAPSHOT: value = steps done, pos3 (vel3 NULL); DONE: value = steps,
  * pos3 and vel3; FAILED: value = the nb_status, no arrays.  The arrays are
- * valid during the call only. */
+ * valid during the call only.  The callback runs on the server's delivery
+ * thread: it may call nb_server_submit, nb_server_job_info and
+ * nb_server_get_stats, but not nb_server_wait or nb_server_destroy (those
+ * wait for that thread), and a slow callback delays the later deliveries. */
 typedef void (*nb_job_fn)(void *user, int64_t job, int32_t event, int32_t value, const float *pos3,
                           const float *vel3, int32_t n);
 void nb_server_config_default(nb_server_config *c);
