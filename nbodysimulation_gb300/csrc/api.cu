@@ -48,6 +48,8 @@ struct nb_sim {
     float4 *wpm = nullptr, *cell_pm = nullptr;
     float4 *cell_q = nullptr, *wqa = nullptr;
     float2 *wqb = nullptr;
+    int *top = nullptr;  // top-level tables: counts, then start entries (kTopRegions each)
+    int top_levels = 0;
     bool quad = false;
     Ctrl *ctrl = nullptr;
     Ctrl *h_ctrl = nullptr;       // pinned mirror for status read-back
@@ -115,8 +117,8 @@ static DevSim dev_view(const nb_sim *s) {
 static void free_tree(nb_sim *s) {
     cudaFree(s->parent); cudaFree(s->child); cudaFree(s->wchild); cudaFree(s->wpm); cudaFree(s->cell_pm);
     cudaFree(s->count); cudaFree(s->start); cudaFree(s->arrive);
-    cudaFree(s->cell_q); cudaFree(s->wqa); cudaFree(s->wqb);
-    s->parent = s->child = s->wchild = s->count = s->start = s->arrive = nullptr;
+    cudaFree(s->cell_q); cudaFree(s->wqa); cudaFree(s->wqb); cudaFree(s->top);
+    s->parent = s->child = s->wchild = s->count = s->start = s->arrive = s->top = nullptr;
     s->wpm = s->cell_pm = s->cell_q = s->wqa = nullptr;
     s->wqb = nullptr;
 }
@@ -137,6 +139,11 @@ static nb_status alloc_tree(nb_sim *s, int cap) {
         NB_CUDA(s, dalloc(&s->cell_q, cells * 2));
         NB_CUDA(s, dalloc(&s->wqa, cells * 8));
         NB_CUDA(s, dalloc(&s->wqb, cells * 8));
+    }
+    s->top_levels = top_levels_for(s->n);
+    if (s->top_levels) {  // the counts start at zero; the build leaves them at zero
+        NB_CUDA(s, dalloc(&s->top, (size_t)2 * kTopRegions));
+        NB_CUDA(s, cudaMemset(s->top, 0, sizeof(int) * kTopRegions));
     }
     return NB_OK;
 }
@@ -412,7 +419,9 @@ static nb_status enqueue_step(nb_sim *s, float dt, int timed) {
         NB_CUDA(s, launch_reset(d, st));
         NB_CUDA(s, launch_bbox(d, s->sm_count, st));
         mark(1);
-        NB_CUDA(s, launch_build(d, p.tree_ref, s->sm_count, st));
+        const TopTables top{s->top, s->top ? s->top + kTopRegions : nullptr, s->top ? s->top_levels : 0};
+        int build_launches = 1;
+        NB_CUDA(s, launch_build(d, top, p.tree_ref, s->sm_count, st, &build_launches));
         mark(2);
         NB_CUDA(s, launch_summarize(d, p.quadrupole, s->sm_count, st));
         mark(3);
@@ -420,7 +429,7 @@ static nb_status enqueue_step(nb_sim *s, float dt, int timed) {
         mark(4);
         NB_CUDA(s, launch_force(d, p, c.precision == NB_PRECISION_COMPENSATED, s->sm_count, st));
         mark(5);
-        s->launches += 6;
+        s->launches += 5 + build_launches;
         for (int k = kStBboxReset; k <= kStForce; ++k) s->stage_ran[k] = true;
     } else {
         const bool quirk = c.force_law == NB_FORCE_REFERENCE_QUIRK;

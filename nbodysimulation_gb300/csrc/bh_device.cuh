@@ -75,20 +75,16 @@ struct RefBox {  // the reference: calculateOctantIdx / adjustBoundaryValues
 // Reference semantics (kRef): the first probe is slot 0 of the super-root
 // without an octant test (build_tree.cl:57-65); the root region is the
 // bounding box; boxes halve as adjustBoundaryValues does.
+//
+// insert_from is the insertion loop: body i (position P) enters slot `slot`
+// of published cell `node` at depth `depth`; g is already that slot's region.
+// insert_body starts it at the root.
 // ---------------------------------------------------------------------------
-template <class Geo, bool kRef>
-__device__ __forceinline__ int insert_body(const DevSim &s, const Geo &root_g, int i, long long spin_cap) {
+template <class Geo>
+__device__ __forceinline__ int insert_from(const DevSim &s, Geo g, int node, int slot, int depth, const float4 P,
+                                           int i, long long spin_cap) {
     Ctrl *ctrl = s.ctrl;
-    const int n = s.n, root = n + s.cap;
-    const float4 P = s.body_cur[i];
-    Geo g = root_g;
-    int node = root, slot, depth = 0;
-    if constexpr (kRef) {
-        slot = 0;
-    } else {
-        slot = g.octant(P.x, P.y, P.z);
-        g.descend(P.x, P.y, P.z);
-    }
+    const int n = s.n;
     int *cslot = &s.child[(node - n) * 8 + slot];
     int ch = ld_volatile(cslot);
     long long spins = 0;
@@ -160,6 +156,38 @@ __device__ __forceinline__ int insert_body(const DevSim &s, const Geo &root_g, i
         }
         ch = ld_volatile(cslot);
     }
+}
+
+template <class Geo, bool kRef>
+__device__ __forceinline__ int insert_body(const DevSim &s, const Geo &root_g, int i, long long spin_cap) {
+    const float4 P = s.body_cur[i];
+    Geo g = root_g;
+    int slot = 0;
+    if constexpr (!kRef) {
+        slot = g.octant(P.x, P.y, P.z);
+        g.descend(P.x, P.y, P.z);
+    }
+    return insert_from<Geo>(s, g, s.n + s.cap, slot, 0, P, i, spin_cap);
+}
+
+// ---------------------------------------------------------------------------
+// Top levels of the cubic-root tree, built before the insertions.  The cell
+// of a region exists in the insertion tree exactly when the region holds at
+// least two bodies, so counting the bodies of every region of level L (8^L
+// regions, the same octant() / descend() steps as an insertion) gives every
+// cell of levels 1..L.  Those cells are allocated level by level (a parent
+// gets a higher index than its children, as in the insertions) and published
+// before the build; each body then starts its insertion at the deepest
+// existing cell of its level-L path.  The tree, its depth and its cell count
+// are the ones the insertions alone give; only the cell numbering differs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int top_region(GeoCube g, const float4 P, int levels) {
+    int id = 0;
+    for (int l = 0; l < levels; ++l) {
+        id = id * 8 + g.octant(P.x, P.y, P.z);
+        g.descend(P.x, P.y, P.z);
+    }
+    return id;
 }
 
 __device__ __forceinline__ void load_children(const int *child, int c, int chs[8], int &nch, int &nbody, int n) {

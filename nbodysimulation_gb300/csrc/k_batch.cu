@@ -173,15 +173,15 @@ __global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
     const int total = t.used_prefix[t.nsys];
     const int stride = gridDim.x * blockDim.x;
     int k = 0, lo = 0, hi = 0;  // the system of the last x and its range (x only grows)
+    int first = 0;              // that system's first allocated cell, read once per system
     for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
         if (x >= hi) {
             k = find_system(t.used_prefix, t.nsys, x);
             lo = t.used_prefix[k];
             hi = t.used_prefix[k + 1];
+            first = t.sys[k].v.ctrl->bottom;
         }
-        const SysDesc &d = t.sys[k];
-        const DevSim s = system_view(d);
-        summarize_from<kQuad>(s, s.ctrl->bottom + (x - lo));
+        summarize_from<kQuad>(system_view(t.sys[k]), first + (x - lo));
     }
 }
 
@@ -195,16 +195,20 @@ __global__ void __launch_bounds__(256) k_batch_sort(BatchTables t) {
     const int total = t.used_prefix[t.nsys];
     const int stride = gridDim.x * blockDim.x;
     int k = 0, lo = 0, hi = 0;  // the system of the last x and its range (x only grows)
+    bool skip = false;          // that system's status and wait limit, read once per system
+    long long cap = 0;
     for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
         if (x >= hi) {
             k = find_system(t.used_prefix, t.nsys, x);
             lo = t.used_prefix[k];
             hi = t.used_prefix[k + 1];
+            const Ctrl *c = t.sys[k].v.ctrl;
+            skip = read_status(c) != 0;
+            cap = tree_spin_cap(c);
         }
-        const SysDesc &d = t.sys[k];
-        const DevSim s = system_view(d);
-        if (read_status(s.ctrl)) continue;
-        sort_cell(s, s.n + s.cap - (x - lo), tree_spin_cap(s.ctrl));
+        if (skip) continue;
+        const DevSim s = system_view(t.sys[k]);
+        if (!sort_cell(s, s.n + s.cap - (x - lo), cap)) skip = true;
     }
 }
 

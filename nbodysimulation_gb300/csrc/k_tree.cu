@@ -7,6 +7,7 @@
 // (kernels/sort.cl).  Each is re-designed for sm_103a; the differences that
 // change results are listed at each kernel.
 #include <algorithm>
+#include <atomic>
 
 #include "bh_device.cuh"
 
@@ -104,6 +105,173 @@ __global__ void __launch_bounds__(256) k_build(DevSim s) {
 }
 
 // ---------------------------------------------------------------------------
+// top levels (cubic-root tree): count, cells, then the build from them.
+// ---------------------------------------------------------------------------
+// Counts per block in shared memory (8^L bins, dynamic), then one global
+// atomic per non-empty bin: regions of a dense centre hold tens of thousands
+// of bodies, which one global counter each would serialise.
+constexpr int kTopCountThreads = 1024;
+__global__ void __launch_bounds__(kTopCountThreads) k_top_count(DevSim s, TopTables t) {
+    extern __shared__ int bins[];
+    Ctrl *ctrl = s.ctrl;
+    if (read_status(ctrl)) return;  // block-uniform, before any barrier
+    const int nbins = 1 << (3 * t.levels);
+    for (int r = threadIdx.x; r < nbins; r += blockDim.x) bins[r] = 0;
+    float box[6];
+    load_box(ctrl, box);
+    const GeoCube root_g = GeoCube::root(box);
+    __syncthreads();
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += stride)
+        atomicAdd(&bins[top_region(root_g, __ldg(&s.body_cur[i]), t.levels)], 1);
+    __syncthreads();
+    for (int r = threadIdx.x; r < nbins; r += blockDim.x)
+        if (bins[r]) atomicAdd(&t.count[r], bins[r]);
+}
+
+// first region of level l (>= 1) in the table of levels 1..4
+__device__ __forceinline__ int top_offset(int l) { return ((1 << (3 * l)) - 8) / 7; }
+
+// Exclusive prefix sum of v over the block (blockDim.x a multiple of 32);
+// *total gets the sum.  Every thread of the block calls it.
+__device__ __forceinline__ int block_exclusive_sum(int v, int *warp_tot, int *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int x = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
+        }
+        if (lane < nw) warp_tot[lane] = x;  // inclusive over warps
+    }
+    __syncthreads();
+    const int before = (w > 0 ? warp_tot[w - 1] : 0) + incl - v;
+    *total = warp_tot[nw - 1];
+    __syncthreads();  // warp_tot is reused by the next call
+    return before;
+}
+
+// One block: region counts of levels L-1..1 from the level-L counts, then
+// the cells of levels 1..L top down, each level's cells numbered below the
+// previous level's (bottom - 1 - rank in region order), then the start
+// entries of the level-L regions.  Clears the level-L counts for the next
+// step in every case.
+constexpr int kTopCellsThreads = 1024;
+__global__ void __launch_bounds__(kTopCellsThreads) k_top_cells(DevSim s, TopTables t) {
+    __shared__ int cnt_sh[kTopInner];   // body counts, regions of levels 1..L-1
+    __shared__ int deep_sh[kTopInner];  // (level << 26) | deepest existing cell of the region's path
+    __shared__ int warp_tot[32];
+    __shared__ int s_skip, s_bottom;
+    Ctrl *ctrl = s.ctrl;
+    const int L = t.levels, n = s.n, root = n + s.cap;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int n_last = 1 << (3 * L);
+    if (tid == 0) {
+        s_skip = read_status(ctrl);
+        s_bottom = ctrl->bottom;
+    }
+    __syncthreads();
+    if (!s_skip) {
+        for (int l = L - 1; l >= 1; --l) {
+            const int nr = 1 << (3 * l);
+            int *dst = cnt_sh + top_offset(l);
+            for (int r = tid; r < nr; r += nt) {
+                int sum = 0;
+                if (l == L - 1) {
+                    const int4 a = reinterpret_cast<const int4 *>(t.count)[2 * r];
+                    const int4 b = reinterpret_cast<const int4 *>(t.count)[2 * r + 1];
+                    sum = a.x + a.y + a.z + a.w + b.x + b.y + b.z + b.w;
+                } else {
+                    const int *src = cnt_sh + top_offset(l + 1) + 8 * r;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) sum += src[j];
+                }
+                dst[r] = sum;
+            }
+            __syncthreads();
+        }
+        for (int l = 1; l <= L; ++l) {
+            // thread tid takes regions tid, tid + nt, ... (coalesced); the
+            // cells of a level are numbered in that order
+            const int nr = 1 << (3 * l);
+            const int *cnt = l < L ? cnt_sh + top_offset(l) : t.count;
+            int mine = 0;
+            for (int r = tid; r < nr; r += nt) mine += cnt[r] >= 2;
+            int total = 0;
+            int rank = block_exclusive_sum(mine, warp_tot, &total);
+            const int bottom = s_bottom;
+            if (bottom - total < n) {  // block-uniform: more top cells than the capacity
+                if (tid == 0) set_status(ctrl, kStCellOverflow, l);
+                s_skip = 1;
+                break;
+            }
+            for (int r = tid; r < nr; r += nt) {
+                const int pe = l == 1 ? root : deep_sh[top_offset(l - 1) + (r >> 3)];
+                int e = pe;
+                if (cnt[r] >= 2) {  // the parent region holds these bodies too: its cell exists
+                    const int cell = bottom - 1 - rank++;
+                    const int c = cell - n;
+                    int4 *row = reinterpret_cast<int4 *>(&s.child[c * 8]);
+                    row[0] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+                    row[1] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+                    const int parent = pe & ((1 << 26) - 1);
+                    s.parent[c] = parent;
+                    s.arrive[c] = 0;
+                    s.start[c] = -1;
+                    s.child[(parent - n) * 8 + (r & 7)] = cell;
+                    e = (l << 26) | cell;
+                }
+                if (l < L) deep_sh[top_offset(l) + r] = e;
+                else t.start[r] = e;
+            }
+            __syncthreads();
+            if (tid == 0) s_bottom = bottom - total;
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    for (int r = tid; r < n_last; r += nt) t.count[r] = 0;
+    if (tid == 0 && !s_skip) ctrl->bottom = s_bottom;
+}
+
+// build from the top levels: each body starts at the deepest existing cell
+// of its level-L path (insert_from), one body per thread, grid-stride
+__global__ void __launch_bounds__(256) k_build_top(DevSim s, TopTables t) {
+    Ctrl *ctrl = s.ctrl;
+    if (read_status(ctrl)) return;
+    float box[6];
+    load_box(ctrl, box);
+    const GeoCube root_g = GeoCube::root(box);
+    int local_max = 0;
+    const long long cap = tree_spin_cap(ctrl);
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += stride) {
+        const float4 P = s.body_cur[i];
+        const int e = __ldg(&t.start[top_region(root_g, P, t.levels)]);
+        const int lv = (int)((unsigned)e >> 26), node = e & ((1 << 26) - 1);
+        GeoCube g = root_g;
+        for (int l = 0; l < lv; ++l) g.descend(P.x, P.y, P.z);
+        const int slot = g.octant(P.x, P.y, P.z);
+        g.descend(P.x, P.y, P.z);
+        const int depth = insert_from<GeoCube>(s, g, node, slot, lv, P, i, cap);
+        if (depth < 0) return;
+        local_max = max(local_max, depth);
+    }
+    const unsigned am = __activemask();
+    const int wmax = __reduce_max_sync(am, local_max);
+    if ((threadIdx.x & 31) == __ffs(am) - 1) atomicMax(&ctrl->max_depth, wmax);
+}
+
+// ---------------------------------------------------------------------------
 // summarize: one cell of [bottom, root] per thread (summarize_from).
 // ---------------------------------------------------------------------------
 template <bool kQuad>
@@ -157,14 +325,41 @@ cudaError_t launch_bbox(const DevSim &s, int sm_count, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_build(const DevSim &s, int tree_ref, int sm_count, cudaStream_t st) {
+cudaError_t launch_build(const DevSim &s, const TopTables &top, int tree_ref, int sm_count, cudaStream_t st,
+                         int *launches) {
+    const int need = (s.n + 255) / 256;
+    if (!tree_ref && top.levels >= 2 && top.levels <= kTopMaxLevels) {
+        const size_t bins_bytes = sizeof(int) << (3 * top.levels);
+        // the 8^5-bin table needs the opt-in shared memory size, set once per device
+        static std::atomic<unsigned long long> bins_attr{0};
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        const unsigned long long bit = 1ull << (dev & 63);
+        if (!(bins_attr.load() & bit)) {
+            e = cudaFuncSetAttribute(k_top_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(int) * kTopRegions));
+            if (e != cudaSuccess) return e;
+            bins_attr.fetch_or(bit);
+        }
+        const int cblocks = std::max(1, std::min(sm_count, (s.n + kTopCountThreads - 1) / kTopCountThreads));
+        k_top_count<<<cblocks, kTopCountThreads, bins_bytes, st>>>(s, top);
+        k_top_cells<<<1, kTopCellsThreads, 0, st>>>(s, top);
+        // two blocks per SM, as for the build from the root (262k-body ball:
+        // 0.12 ms against 0.14 ms on the whole co-resident grid; 4M: equal)
+        int blocks = std::min(resident_blocks((const void *)k_build_top, 256, sm_count), 2 * sm_count);
+        if (blocks > need) blocks = need > 0 ? need : 1;
+        k_build_top<<<blocks, 256, 0, st>>>(s, top);
+        *launches = 3;
+        return cudaGetLastError();
+    }
+    *launches = 1;
     const void *fn = tree_ref ? (const void *)k_build<RefBox, true> : (const void *)k_build<GeoCube, false>;
     // two blocks per SM: threads that start at the root together contend for
     // its first cells, and fewer of them insert faster (measured build time
     // with 1 / 2 / 4 / 8 blocks per SM: 262k-body ball 0.20 / 0.20 / 0.30 /
     // 0.32 ms, 1M 0.60 / 0.41 / 0.49 / 0.54 ms, 4M 2.25 / 1.26 / 1.24 / 1.32 ms)
     int blocks = std::min(resident_blocks(fn, 256, sm_count), 2 * sm_count);
-    const int need = (s.n + 255) / 256;
     if (blocks > need) blocks = need > 0 ? need : 1;
     if (tree_ref) k_build<RefBox, true><<<blocks, 256, 0, st>>>(s);
     else k_build<GeoCube, false><<<blocks, 256, 0, st>>>(s);

@@ -204,7 +204,29 @@ struct LaunchShape {
 
 cudaError_t launch_reset(const DevSim &s, cudaStream_t st);
 cudaError_t launch_bbox(const DevSim &s, int sm_count, cudaStream_t st);
-cudaError_t launch_build(const DevSim &s, int tree_ref, int sm_count, cudaStream_t st);
+// Per-system tables of the top levels of the cubic-root tree (k_tree.cu):
+// body counts of the 8^levels regions of the deepest top level (zero between
+// steps) and, per region, the packed (level << 26) | cell its bodies start
+// their insertion at.  levels = 0: every insertion starts at the root.
+struct TopTables {
+    int *count;
+    int *start;
+    int levels;
+};
+constexpr int kTopMaxLevels = 5;                  // 8^5 = 32768 regions
+constexpr int kTopRegions = 1 << (3 * kTopMaxLevels);
+constexpr int kTopInner = (kTopRegions - 8) / 7;  // regions of levels 1..4: 8 + 64 + 512 + 4096
+// top levels for a tree of n bodies: about 32 bodies or more per region of the
+// deepest level, at most kTopMaxLevels, none below 2
+inline int top_levels_for(int n) {
+    int l = 0;
+    while (l < kTopMaxLevels && (32LL << (3 * (l + 1))) <= (long long)n) ++l;
+    return l >= 2 ? l : 0;
+}
+// Launches the build (the top-level count and cells first when top.levels >
+// 0 and the tree is the cubic-root one); *launches gets the kernel count.
+cudaError_t launch_build(const DevSim &s, const TopTables &top, int tree_ref, int sm_count, cudaStream_t st,
+                         int *launches);
 cudaError_t launch_summarize(const DevSim &s, int quadrupole, int sm_count, cudaStream_t st);
 cudaError_t launch_sort(const DevSim &s, int sm_count, cudaStream_t st);
 cudaError_t launch_force(const DevSim &s, const StepParams &p, int compensated, int sm_count, cudaStream_t st);
