@@ -210,6 +210,10 @@ nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out) {
         cudaMemset(m.vel, 0, sizeof(float4) * m.n);
         cudaMemset(m.acc, 0, sizeof(float4) * m.n);
         cudaMemset(m.body[0], 0, sizeof(float4) * m.n);
+        int *top_counts = nullptr;
+        size_t top_bytes = 0;
+        sysmem_top_counts(m, &top_counts, &top_bytes);
+        if (top_bytes) cudaMemset(top_counts, 0, top_bytes);
         b->h_sys[k] = sysmem_desc(m, cfgs[k], 0.0f);
     }
     if (cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess) return fail_all(NB_ERR_CUDA);

@@ -190,6 +190,146 @@ __device__ __forceinline__ int top_region(GeoCube g, const float4 P, int levels)
     return id;
 }
 
+// first region of level l (>= 1) in a table of the regions of levels 1..4
+__device__ __forceinline__ int top_offset(int l) { return ((1 << (3 * l)) - 8) / 7; }
+
+// Exclusive prefix sum of v over the block (blockDim.x a multiple of 32,
+// at most 1024); *total gets the sum.  Every thread of the block calls it.
+__device__ __forceinline__ int block_exclusive_sum(int v, int *warp_tot, int *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int x = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
+        }
+        if (lane < nw) warp_tot[lane] = x;  // inclusive over warps
+    }
+    __syncthreads();
+    const int before = (w > 0 ? warp_tot[w - 1] : 0) + incl - v;
+    *total = warp_tot[nw - 1];
+    __syncthreads();  // warp_tot is reused by the next call
+    return before;
+}
+
+// Level-L region counts of bodies [i0 + threadIdx.x, i1) with stride `stride`
+// into the block's shared bins (8^L ints), then one global atomic per
+// non-empty bin.  Every thread of the block calls it.
+__device__ __forceinline__ void top_count_range(const DevSim &s, const TopTables &t, const GeoCube &root_g, int i0,
+                                                int i1, int stride, int *bins) {
+    const int nbins = 1 << (3 * t.levels);
+    for (int r = threadIdx.x; r < nbins; r += blockDim.x) bins[r] = 0;
+    __syncthreads();
+    for (int i = i0 + threadIdx.x; i < i1; i += stride)
+        atomicAdd(&bins[top_region(root_g, __ldg(&s.body_cur[i]), t.levels)], 1);
+    __syncthreads();
+    for (int r = threadIdx.x; r < nbins; r += blockDim.x)
+        if (bins[r]) atomicAdd(&t.count[r], bins[r]);
+}
+
+// One block: region counts of levels L-1..1 from the level-L counts, then
+// the cells of levels 1..L top down (thread tid takes regions tid, tid + nt,
+// ...; a level's cells are numbered bottom - 1 - rank in that order, below
+// the previous level's), then the start entry of every level-L region.
+// Clears the level-L counts for the next step in every case.  Every thread
+// of the block calls it.
+__device__ __forceinline__ void top_cells_block(const DevSim &s, const TopTables &t) {
+    __shared__ int cnt_sh[kTopInner];   // body counts, regions of levels 1..L-1
+    __shared__ int deep_sh[kTopInner];  // (level << 26) | deepest existing cell of the region's path
+    __shared__ int warp_tot[32];
+    __shared__ int s_skip, s_bottom;
+    Ctrl *ctrl = s.ctrl;
+    const int L = t.levels, n = s.n, root = n + s.cap;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int n_last = 1 << (3 * L);
+    if (tid == 0) {
+        s_skip = read_status(ctrl);
+        s_bottom = ctrl->bottom;
+    }
+    __syncthreads();
+    if (!s_skip) {
+        for (int l = L - 1; l >= 1; --l) {
+            const int nr = 1 << (3 * l);
+            int *dst = cnt_sh + top_offset(l);
+            for (int r = tid; r < nr; r += nt) {
+                int sum = 0;
+                if (l == L - 1) {
+                    const int4 a = reinterpret_cast<const int4 *>(t.count)[2 * r];
+                    const int4 b = reinterpret_cast<const int4 *>(t.count)[2 * r + 1];
+                    sum = a.x + a.y + a.z + a.w + b.x + b.y + b.z + b.w;
+                } else {
+                    const int *src = cnt_sh + top_offset(l + 1) + 8 * r;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) sum += src[j];
+                }
+                dst[r] = sum;
+            }
+            __syncthreads();
+        }
+        for (int l = 1; l <= L; ++l) {
+            const int nr = 1 << (3 * l);
+            const int *cnt = l < L ? cnt_sh + top_offset(l) : t.count;
+            int mine = 0;
+            for (int r = tid; r < nr; r += nt) mine += cnt[r] >= 2;
+            int total = 0;
+            int rank = block_exclusive_sum(mine, warp_tot, &total);
+            const int bottom = s_bottom;
+            if (bottom - total < n) {  // block-uniform: more top cells than the capacity
+                if (tid == 0) set_status(ctrl, kStCellOverflow, l);
+                s_skip = 1;
+                break;
+            }
+            for (int r = tid; r < nr; r += nt) {
+                const int pe = l == 1 ? root : deep_sh[top_offset(l - 1) + (r >> 3)];
+                int e = pe;
+                if (cnt[r] >= 2) {  // the parent region holds these bodies too: its cell exists
+                    const int cell = bottom - 1 - rank++;
+                    const int c = cell - n;
+                    int4 *row = reinterpret_cast<int4 *>(&s.child[c * 8]);
+                    row[0] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+                    row[1] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+                    const int parent = pe & ((1 << 26) - 1);
+                    s.parent[c] = parent;
+                    s.arrive[c] = 0;
+                    s.start[c] = -1;
+                    s.child[(parent - n) * 8 + (r & 7)] = cell;
+                    e = (l << 26) | cell;
+                }
+                if (l < L) deep_sh[top_offset(l) + r] = e;
+                else t.start[r] = e;
+            }
+            __syncthreads();
+            if (tid == 0) s_bottom = bottom - total;
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    for (int r = tid; r < n_last; r += nt) t.count[r] = 0;
+    if (tid == 0 && !s_skip) ctrl->bottom = s_bottom;
+}
+
+// Insertion of body i from the deepest existing top cell of its level-L path.
+__device__ __forceinline__ int insert_from_top(const DevSim &s, const TopTables &t, const GeoCube &root_g, int i,
+                                               long long spin_cap) {
+    const float4 P = s.body_cur[i];
+    const int e = __ldg(&t.start[top_region(root_g, P, t.levels)]);
+    const int lv = (int)((unsigned)e >> 26), node = e & ((1 << 26) - 1);
+    GeoCube g = root_g;
+    for (int l = 0; l < lv; ++l) g.descend(P.x, P.y, P.z);
+    const int slot = g.octant(P.x, P.y, P.z);
+    g.descend(P.x, P.y, P.z);
+    return insert_from<GeoCube>(s, g, node, slot, lv, P, i, spin_cap);
+}
+
 __device__ __forceinline__ void load_children(const int *child, int c, int chs[8], int &nch, int &nbody, int n) {
     const int4 a0 = *reinterpret_cast<const int4 *>(&child[c * 8]);
     const int4 a1 = *reinterpret_cast<const int4 *>(&child[c * 8 + 4]);

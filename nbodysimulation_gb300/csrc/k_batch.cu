@@ -5,9 +5,9 @@
 // finds its system with a binary search in the stage's prefix table.
 // Barnes-Hut systems run the same per-item code as the single-system
 // kernels (bh_device.cuh, force_device.cuh); small systems take the
-// TMA-tiled direct sum.  A step is: reset, bbox, build, used-cell scan,
-// summarize, sort, force, direct, flip -- captured once into a CUDA graph by
-// the host.
+// TMA-tiled direct sum.  A step is: reset, bbox, top-level counts, top cells,
+// build, used-cell scan, summarize, sort, force, direct, flip -- captured
+// once into a CUDA graph by the host.
 #include "bh_device.cuh"
 #include "force_device.cuh"
 #include "tma.cuh"
@@ -102,6 +102,46 @@ __device__ __forceinline__ int build_chunk(const DevSim &s, int i0, int i1) {
     return local_max;
 }
 
+// the same from the top levels (insert_from_top)
+__device__ __forceinline__ int build_chunk_top(const DevSim &s, const TopTables &top, int i0, int i1) {
+    float box[6];
+    load_box(s.ctrl, box);
+    const GeoCube root_g = GeoCube::root(box);
+    int local_max = 0;
+    const long long cap = tree_spin_cap(s.ctrl);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int depth = insert_from_top(s, top, root_g, i, cap);
+        if (depth < 0) return -1;
+        local_max = max(local_max, depth);
+    }
+    return local_max;
+}
+
+// ---------------------------------------------------------------------------
+// top levels of every cubic-root tree that has them (top_levels): region
+// counts per chunk of bodies in shared-memory bins, then one block per tree
+// creates its top cells (top_cells_block); the build then starts every
+// insertion below them
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_batch_top_count(BatchTables t) {
+    __shared__ int bins[1 << (3 * kBatchTopMaxLevels)];
+    const int k = find_system(t.chunk_prefix, t.nsys, blockIdx.x);
+    const SysDesc &d = t.sys[k];
+    // block-uniform, before any barrier: only earlier kernels set the status
+    if (d.top.levels == 0 || !system_live(d.v.ctrl) || read_status(d.v.ctrl)) return;
+    const DevSim s = system_view(d);
+    float box[6];
+    load_box(s.ctrl, box);
+    const int i0 = (blockIdx.x - d.chunk_begin) * d.chunk;
+    top_count_range(s, d.top, GeoCube::root(box), i0, min(s.n, i0 + d.chunk), blockDim.x, bins);
+}
+
+__global__ void __launch_bounds__(256) k_batch_top_cells(BatchTables t) {
+    const SysDesc &d = t.sys[blockIdx.x];
+    if (!d.active || d.kind != kSysBH || d.top.levels == 0 || !system_live(d.v.ctrl)) return;
+    top_cells_block(system_view(d), d.top);
+}
+
 __global__ void __launch_bounds__(256) k_batch_build(BatchTables t) {
     const int k = find_system(t.chunk_prefix, t.nsys, blockIdx.x);
     const SysDesc &d = t.sys[k];
@@ -109,7 +149,9 @@ __global__ void __launch_bounds__(256) k_batch_build(BatchTables t) {
     if (read_status(s.ctrl) || !system_live(s.ctrl)) return;
     const int i0 = (blockIdx.x - d.chunk_begin) * d.chunk;
     const int i1 = min(s.n, i0 + d.chunk);
-    const int depth = d.p.tree_ref ? build_chunk<RefBox, true>(s, i0, i1) : build_chunk<GeoCube, false>(s, i0, i1);
+    const int depth = d.p.tree_ref     ? build_chunk<RefBox, true>(s, i0, i1)
+                      : d.top.levels ? build_chunk_top(s, d.top, i0, i1)
+                                     : build_chunk<GeoCube, false>(s, i0, i1);
     if (depth < 0) return;
     const unsigned am = __activemask();
     const int wmax = __reduce_max_sync(am, depth);
@@ -457,6 +499,8 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
     if (t.chunks > 0) {
         k_batch_reset<<<sb, 128, 0, st>>>(t);
         k_batch_bbox<<<t.chunks, 256, 0, st>>>(t);
+        k_batch_top_count<<<t.chunks, 256, 0, st>>>(t);
+        k_batch_top_cells<<<t.nsys, 256, 0, st>>>(t);
         k_batch_build<<<t.chunks, 256, 0, st>>>(t);
         k_batch_used<<<1, kScanThreads, 0, st>>>(t);
         int sblocks = sm_count * 8;
@@ -475,7 +519,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
         default: e = launch_batch_force_m<0>(t, comp, quad, sm_count, st); break;
         }
         if (e != cudaSuccess) return e;
-        nl += 7;
+        nl += 9;
     }
     if (t.dblocks > 0) {
         if ((e = launch_direct_variant(t, direct_variant, st)) != cudaSuccess) return e;

@@ -151,6 +151,33 @@ __device__ __forceinline__ void load_box(const Ctrl *c, float box[6]) {
 // One system of a batch (nb_batch / nb_server): its buffers, its step
 // parameters and where its work starts in the batch-wide index spaces.
 enum SysKind { kSysBH = 0, kSysDirect = 1 };
+// Per-system tables of the top levels of the cubic-root tree (k_tree.cu):
+// body counts of the 8^levels regions of the deepest top level (zero between
+// steps) and, per region, the packed (level << 26) | cell its bodies start
+// their insertion at.  levels = 0: every insertion starts at the root.
+struct TopTables {
+    int *count;
+    int *start;
+    int levels;
+};
+constexpr int kTopMaxLevels = 5;                  // 8^5 = 32768 regions
+constexpr int kTopRegions = 1 << (3 * kTopMaxLevels);
+constexpr int kTopInner = (kTopRegions - 8) / 7;  // regions of levels 1..4: 8 + 64 + 512 + 4096
+// top levels for a tree of n bodies: about 32 bodies or more per region of the
+// deepest level, at most kTopMaxLevels, none below 2
+inline int top_levels_for(int n) {
+    int l = 0;
+    while (l < kTopMaxLevels && (32LL << (3 * (l + 1))) <= (long long)n) ++l;
+    return l >= 2 ? l : 0;
+}
+// batched trees count in shared-memory bins per block of bodies, so at most
+// 4 levels (4096 bins, 16 KB)
+constexpr int kBatchTopMaxLevels = 4;
+inline int batch_top_levels_for(int n) {
+    const int l = top_levels_for(n);
+    return l < kBatchTopMaxLevels ? l : kBatchTopMaxLevels;
+}
+
 struct SysDesc {
     DevSim v;          // pointers; body_cur / body_next come from body[] and ctrl->parity
     float4 *body[2];
@@ -163,6 +190,7 @@ struct SysDesc {
     int group_begin;   // prefix over BH systems' warp groups
     int dblock_begin;  // prefix over direct systems' target blocks
     int chunk;         // bodies per bbox / build block (batch_chunk)
+    TopTables top;     // top-level tables; levels = 0: insertions from the root
 };
 
 // Prefix tables (nsys + 1 entries each) and totals of a batch.
@@ -204,25 +232,6 @@ struct LaunchShape {
 
 cudaError_t launch_reset(const DevSim &s, cudaStream_t st);
 cudaError_t launch_bbox(const DevSim &s, int sm_count, cudaStream_t st);
-// Per-system tables of the top levels of the cubic-root tree (k_tree.cu):
-// body counts of the 8^levels regions of the deepest top level (zero between
-// steps) and, per region, the packed (level << 26) | cell its bodies start
-// their insertion at.  levels = 0: every insertion starts at the root.
-struct TopTables {
-    int *count;
-    int *start;
-    int levels;
-};
-constexpr int kTopMaxLevels = 5;                  // 8^5 = 32768 regions
-constexpr int kTopRegions = 1 << (3 * kTopMaxLevels);
-constexpr int kTopInner = (kTopRegions - 8) / 7;  // regions of levels 1..4: 8 + 64 + 512 + 4096
-// top levels for a tree of n bodies: about 32 bodies or more per region of the
-// deepest level, at most kTopMaxLevels, none below 2
-inline int top_levels_for(int n) {
-    int l = 0;
-    while (l < kTopMaxLevels && (32LL << (3 * (l + 1))) <= (long long)n) ++l;
-    return l >= 2 ? l : 0;
-}
 // Launches the build (the top-level count and cells first when top.levels >
 // 0 and the tree is the cubic-root one); *launches gets the kernel count.
 cudaError_t launch_build(const DevSim &s, const TopTables &top, int tree_ref, int sm_count, cudaStream_t st,

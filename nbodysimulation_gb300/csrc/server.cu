@@ -172,6 +172,10 @@ static cudaError_t upload_job(nb_server *s, Job &j, char *&stage, size_t &stage_
         (e = cudaMemsetAsync(j.mem.acc, 0, 16 * n, s->upload)) != cudaSuccess ||
         (e = cudaMemcpyAsync(j.mem.ctrl, init, sizeof(Ctrl), cudaMemcpyHostToDevice, s->upload)) != cudaSuccess)
         return e;
+    int *top_counts = nullptr;
+    size_t top_bytes = 0;
+    sysmem_top_counts(j.mem, &top_counts, &top_bytes);
+    if (top_bytes && (e = cudaMemsetAsync(top_counts, 0, top_bytes, s->upload)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&j.uploaded, cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(j.uploaded, s->upload)) != cudaSuccess) return e;
     j.desc = sysmem_desc(j.mem, j.cfg, j.dt);

@@ -19,6 +19,8 @@ struct SysMem {
         *arrive = nullptr, *sorted = nullptr;
     float4 *wpm = nullptr, *cell_pm = nullptr, *cell_q = nullptr, *wqa = nullptr;
     float2 *wqb = nullptr;
+    int *top = nullptr;  // top-level tables (batch_top_levels_for): counts, then start entries
+    int top_levels = 0;
     Ctrl *ctrl = nullptr;
 };
 
@@ -34,7 +36,9 @@ inline int sysmem_default_capacity(int n) {
 }
 
 // Bytes the system needs; when base is non-null the pointers are set to
-// consecutive pieces of [base, base + bytes).
+// consecutive pieces of [base, base + bytes).  The owner clears the top-level
+// counts (sysmem_top_counts) once before the first step; every step leaves
+// them at zero.
 inline size_t sysmem_layout(SysMem &m, char *base) {
     size_t off = 0;
     auto take = [&](auto *&p, size_t count) {
@@ -64,8 +68,16 @@ inline size_t sysmem_layout(SysMem &m, char *base) {
             take(m.wqa, cells * 8);
             take(m.wqb, cells * 8);
         }
+        m.top_levels = batch_top_levels_for(m.n);
+        if (m.top_levels) take(m.top, (size_t)2 << (3 * m.top_levels));
     }
     return sysmem_align(off);
+}
+
+// the top-level count table of a tree (nullptr, 0 when it has none)
+inline void sysmem_top_counts(const SysMem &m, int **p, size_t *bytes) {
+    *p = m.top;
+    *bytes = m.top ? sizeof(int) << (3 * m.top_levels) : 0;
 }
 
 inline size_t sysmem_bytes(int n, bool tree, bool quad, int cap) {
@@ -102,6 +114,9 @@ inline SysDesc sysmem_desc(const SysMem &m, const nb_config &c, float dt) {
     v.wqa = m.wqa;
     v.wqb = m.wqb;
     v.ctrl = m.ctrl;
+    // the reference tree semantics always insert from the root
+    const int top = c.tree_semantics == NB_TREE_REFERENCE ? 0 : m.top_levels;
+    d.top = TopTables{top ? m.top : nullptr, top ? m.top + (1 << (3 * top)) : nullptr, top};
     d.body[0] = m.body[0];
     d.body[1] = m.body[1];
     StepParams &p = d.p;
