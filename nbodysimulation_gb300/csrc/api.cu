@@ -48,7 +48,7 @@ struct nb_sim {
     float4 *wpm = nullptr, *cell_pm = nullptr;
     float4 *cell_q = nullptr, *wqa = nullptr;
     float2 *wqb = nullptr;
-    int *top = nullptr;  // top-level tables: counts, then start entries (kTopRegions each)
+    int *top = nullptr;  // top-level tables: counts, start entries (kTopRegions each), level L-1 entries
     int top_levels = 0;
     bool quad = false;
     Ctrl *ctrl = nullptr;
@@ -142,7 +142,7 @@ static nb_status alloc_tree(nb_sim *s, int cap) {
     }
     s->top_levels = top_levels_for(s->n);
     if (s->top_levels) {  // the counts start at zero; the build leaves them at zero
-        NB_CUDA(s, dalloc(&s->top, (size_t)2 * kTopRegions));
+        NB_CUDA(s, dalloc(&s->top, (size_t)2 * kTopRegions + kTopRegions / 8));
         NB_CUDA(s, cudaMemset(s->top, 0, sizeof(int) * kTopRegions));
     }
     return NB_OK;
@@ -419,7 +419,8 @@ static nb_status enqueue_step(nb_sim *s, float dt, int timed) {
         NB_CUDA(s, launch_reset(d, st));
         NB_CUDA(s, launch_bbox(d, s->sm_count, st));
         mark(1);
-        const TopTables top{s->top, s->top ? s->top + kTopRegions : nullptr, s->top ? s->top_levels : 0};
+        const TopTables top{s->top, s->top ? s->top + kTopRegions : nullptr, s->top ? s->top_levels : 0,
+                            s->top ? s->top + 2 * kTopRegions : nullptr};
         int build_launches = 1;
         NB_CUDA(s, launch_build(d, top, p.tree_ref, s->sm_count, st, &build_launches));
         mark(2);

@@ -237,14 +237,18 @@ __device__ __forceinline__ void top_count_range(const DevSim &s, const TopTables
 }
 
 // One block: region counts of levels L-1..1 from the level-L counts, then
-// the cells of levels 1..L top down (thread tid takes regions tid, tid + nt,
-// ...; a level's cells are numbered bottom - 1 - rank in that order, below
-// the previous level's), then the start entry of every level-L region.
-// Clears the level-L counts for the next step in every case.  Every thread
-// of the block calls it.
-__device__ __forceinline__ void top_cells_block(const DevSim &s, const TopTables &t) {
+// the cells of levels 1..L top down (each level's cells numbered below the
+// previous level's), then the start entry of every level-L region.  Clears
+// the level-L counts for the next step in every case.  With deep_out, the
+// block stops after level L-1 and leaves that level's entries in deep_out
+// (8^(L-1) ints) and the counts in place for top_leaf_cells.  Every thread of
+// the block calls it; blockDim.x is a power of two with 8^L <= 32 *
+// blockDim.x, so a thread takes at most 32 regions of a level and a level has
+// at most kTopRegions / 32 (round, warp) pairs.
+__device__ __forceinline__ void top_cells_block(const DevSim &s, const TopTables &t, int *deep_out = nullptr) {
     __shared__ int cnt_sh[kTopInner];   // body counts, regions of levels 1..L-1
     __shared__ int deep_sh[kTopInner];  // (level << 26) | deepest existing cell of the region's path
+    __shared__ int rank_sh[kTopRegions / 32];  // per (round, warp): new cells before it
     __shared__ int warp_tot[32];
     __shared__ int s_skip, s_bottom;
     Ctrl *ctrl = s.ctrl;
@@ -275,24 +279,51 @@ __device__ __forceinline__ void top_cells_block(const DevSim &s, const TopTables
             }
             __syncthreads();
         }
-        for (int l = 1; l <= L; ++l) {
+        const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+        const unsigned below = (1u << lane) - 1u;
+        const int last = deep_out ? L - 1 : L;
+        for (int l = 1; l <= last; ++l) {
+            // region r = j * nt + tid in round j; a level's cells are numbered
+            // bottom - 1 - rank with rank in (round, warp, lane) order, so a
+            // warp's new cells are consecutive and its writes coalesce
             const int nr = 1 << (3 * l);
+            const int rounds = (nr + nt - 1) / nt, m = rounds * nw;  // rounds <= 32: 8^L <= 32 * blockDim.x
             const int *cnt = l < L ? cnt_sh + top_offset(l) : t.count;
-            int mine = 0;
-            for (int r = tid; r < nr; r += nt) mine += cnt[r] >= 2;
-            int total = 0;
-            int rank = block_exclusive_sum(mine, warp_tot, &total);
+            unsigned make_bits = 0;  // bit j: region j * nt + tid gets a cell
+#pragma unroll 8
+            for (int j = 0; j < rounds; ++j) {  // independent loads, then the votes
+                const int r = j * nt + tid;
+                if (r < nr && cnt[r] >= 2) make_bits |= 1u << j;
+            }
+            for (int j = 0; j < rounds; ++j) {
+                const unsigned b = __ballot_sync(0xffffffffu, (make_bits >> j) & 1u);
+                if (lane == 0) rank_sh[j * nw + w] = __popc(b);
+            }
+            __syncthreads();
+            int total = 0;  // exclusive scan of rank_sh[0, m) in place
+            for (int base = 0; base < m; base += nt) {
+                const int v = base + tid < m ? rank_sh[base + tid] : 0;
+                int part = 0;
+                const int ex = block_exclusive_sum(v, warp_tot, &part);
+                if (base + tid < m) rank_sh[base + tid] = total + ex;
+                total += part;
+            }
+            __syncthreads();
             const int bottom = s_bottom;
             if (bottom - total < n) {  // block-uniform: more top cells than the capacity
                 if (tid == 0) set_status(ctrl, kStCellOverflow, l);
                 s_skip = 1;
                 break;
             }
-            for (int r = tid; r < nr; r += nt) {
+            for (int j = 0; j < rounds; ++j) {
+                const int r = j * nt + tid;
+                const bool make = (make_bits >> j) & 1u;
+                const unsigned b = __ballot_sync(0xffffffffu, make);
+                if (r >= nr) continue;
                 const int pe = l == 1 ? root : deep_sh[top_offset(l - 1) + (r >> 3)];
                 int e = pe;
-                if (cnt[r] >= 2) {  // the parent region holds these bodies too: its cell exists
-                    const int cell = bottom - 1 - rank++;
+                if (make) {  // the parent region holds these bodies too: its cell exists
+                    const int cell = bottom - 1 - (rank_sh[j * nw + w] + __popc(b & below));
                     const int c = cell - n;
                     int4 *row = reinterpret_cast<int4 *>(&s.child[c * 8]);
                     row[0] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
@@ -306,6 +337,7 @@ __device__ __forceinline__ void top_cells_block(const DevSim &s, const TopTables
                 }
                 if (l < L) deep_sh[top_offset(l) + r] = e;
                 else t.start[r] = e;
+                if (deep_out && l == last) deep_out[r] = e;
             }
             __syncthreads();
             if (tid == 0) s_bottom = bottom - total;
@@ -313,8 +345,49 @@ __device__ __forceinline__ void top_cells_block(const DevSim &s, const TopTables
         }
     }
     __syncthreads();
-    for (int r = tid; r < n_last; r += nt) t.count[r] = 0;
+    if (!deep_out)
+        for (int r = tid; r < n_last; r += nt) t.count[r] = 0;
     if (tid == 0 && !s_skip) ctrl->bottom = s_bottom;
+}
+
+// The cells of level L after top_cells_block(..., deep): one region per
+// thread, warp-aggregated numbering from the cell counter (below every cell
+// of the upper levels), the start entries, and the counts cleared.
+__device__ __forceinline__ void top_leaf_cells(const DevSim &s, const TopTables &t, const int *deep, int r) {
+    Ctrl *ctrl = s.ctrl;
+    const int n = s.n, nr = 1 << (3 * t.levels);
+    const bool skip = read_status(ctrl) != 0;  // grid-uniform: only earlier kernels set it
+    const int cnt = r < nr ? t.count[r] : 0;
+    const bool make = !skip && cnt >= 2;
+    const unsigned am = __activemask();
+    const unsigned b = __ballot_sync(am, make);
+    const int leader = __ffs(am) - 1, lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == leader && b) base = atomicSub(&ctrl->bottom, __popc(b));
+    base = __shfl_sync(am, base, leader);
+    if (r >= nr) return;
+    t.count[r] = 0;
+    if (skip) return;
+    const int pe = deep[r >> 3];
+    int e = pe;
+    if (make) {
+        const int cell = base - 1 - __popc(b & ((1u << lane) - 1u));
+        if (cell < n) {  // more top cells than the capacity
+            set_status(ctrl, kStCellOverflow, t.levels);
+            return;
+        }
+        const int c = cell - n;
+        int4 *row = reinterpret_cast<int4 *>(&s.child[c * 8]);
+        row[0] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+        row[1] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+        const int parent = pe & ((1 << 26) - 1);
+        s.parent[c] = parent;
+        s.arrive[c] = 0;
+        s.start[c] = -1;
+        s.child[(parent - n) * 8 + (r & 7)] = cell;
+        e = (t.levels << 26) | cell;
+    }
+    t.start[r] = e;
 }
 
 // Insertion of body i from the deepest existing top cell of its level-L path.

@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(256) k_batch_top_count(BatchTables t) {
     top_count_range(s, d.top, GeoCube::root(box), i0, min(s.n, i0 + d.chunk), blockDim.x, bins);
 }
 
+static_assert((1 << (3 * kBatchTopMaxLevels)) <= 32 * 256, "top_cells_block: at most 32 regions a thread");
 __global__ void __launch_bounds__(256) k_batch_top_cells(BatchTables t) {
     const SysDesc &d = t.sys[blockIdx.x];
     if (!d.active || d.kind != kSysBH || d.top.levels == 0 || !system_live(d.v.ctrl)) return;
@@ -215,15 +216,16 @@ __global__ void __launch_bounds__(256) k_batch_summarize(BatchTables t) {
     const int total = t.used_prefix[t.nsys];
     const int stride = gridDim.x * blockDim.x;
     int k = 0, lo = 0, hi = 0;  // the system of the last x and its range (x only grows)
-    int first = 0;              // that system's first allocated cell, read once per system
+    int first = 0, par = 0;     // that system's first allocated cell and buffer parity, read once
     for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
         if (x >= hi) {
             k = find_system(t.used_prefix, t.nsys, x);
             lo = t.used_prefix[k];
             hi = t.used_prefix[k + 1];
             first = t.sys[k].v.ctrl->bottom;
+            par = system_parity(t.sys[k]);
         }
-        summarize_from<kQuad>(system_view(t.sys[k]), first + (x - lo));
+        summarize_from<kQuad>(system_view_par(t.sys[k], par), first + (x - lo));
     }
 }
 
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(256) k_batch_sort(BatchTables t) {
             cap = tree_spin_cap(c);
         }
         if (skip) continue;
-        const DevSim s = system_view(t.sys[k]);
+        const DevSim &s = t.sys[k].v;  // the sort reads no body buffer
         if (!sort_cell(s, s.n + s.cap - (x - lo), cap)) skip = true;
     }
 }

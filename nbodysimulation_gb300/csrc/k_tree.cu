@@ -121,7 +121,15 @@ __global__ void __launch_bounds__(kTopCountThreads) k_top_count(DevSim s, TopTab
 }
 
 constexpr int kTopCellsThreads = 1024;
-__global__ void __launch_bounds__(kTopCellsThreads) k_top_cells(DevSim s, TopTables t) { top_cells_block(s, t); }
+static_assert((1 << (3 * kTopMaxLevels)) <= 32 * kTopCellsThreads, "top_cells_block: at most 32 regions a thread");
+// levels 1..L-1 in one block, then level L (most of the cells) over a grid
+__global__ void __launch_bounds__(kTopCellsThreads) k_top_cells(DevSim s, TopTables t) {
+    top_cells_block(s, t, t.deep);
+}
+
+__global__ void __launch_bounds__(256) k_top_leaf(DevSim s, TopTables t) {
+    top_leaf_cells(s, t, t.deep, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // build from the top levels, one body per thread, grid-stride
 __global__ void __launch_bounds__(256) k_build_top(DevSim s, TopTables t) {
@@ -216,13 +224,14 @@ cudaError_t launch_build(const DevSim &s, const TopTables &top, int tree_ref, in
         }
         const int cblocks = std::max(1, std::min(sm_count, (s.n + kTopCountThreads - 1) / kTopCountThreads));
         k_top_count<<<cblocks, kTopCountThreads, bins_bytes, st>>>(s, top);
-        k_top_cells<<<1, kTopCellsThreads, 0, st>>>(s, top);
+        k_top_cells<<<1, kTopCellsThreads, 0, st>>>(s, top);  // all levels in the block when top.deep is null
+        if (top.deep) k_top_leaf<<<((1 << (3 * top.levels)) + 255) / 256, 256, 0, st>>>(s, top);
         // two blocks per SM, as for the build from the root (262k-body ball:
         // 0.12 ms against 0.14 ms on the whole co-resident grid; 4M: equal)
         int blocks = std::min(resident_blocks((const void *)k_build_top, 256, sm_count), 2 * sm_count);
         if (blocks > need) blocks = need > 0 ? need : 1;
         k_build_top<<<blocks, 256, 0, st>>>(s, top);
-        *launches = 3;
+        *launches = top.deep ? 4 : 3;
         return cudaGetLastError();
     }
     *launches = 1;

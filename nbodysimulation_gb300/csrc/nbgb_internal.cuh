@@ -159,6 +159,7 @@ struct TopTables {
     int *count;
     int *start;
     int levels;
+    int *deep;  // 8^(levels-1) entries of level levels-1 when the last level is built by a grid (else null)
 };
 constexpr int kTopMaxLevels = 5;                  // 8^5 = 32768 regions
 constexpr int kTopRegions = 1 << (3 * kTopMaxLevels);
@@ -216,13 +217,16 @@ __device__ __forceinline__ int find_system(const int *prefix, int nsys, int x) {
 // A batched system with no steps left takes no part in any stage.
 __device__ __forceinline__ bool system_live(const Ctrl *c) { return ld_volatile(&c->budget) != 0; }
 
-__device__ __forceinline__ DevSim system_view(const SysDesc &d) {
+__device__ __forceinline__ DevSim system_view_par(const SysDesc &d, int par) {
     DevSim v = d.v;
-    const int par = ld_volatile(&v.ctrl->parity) & 1;
     v.body_cur = d.body[par];
     v.body_next = d.body[par ^ 1];
     return v;
 }
+
+__device__ __forceinline__ int system_parity(const SysDesc &d) { return ld_volatile(&d.v.ctrl->parity) & 1; }
+
+__device__ __forceinline__ DevSim system_view(const SysDesc &d) { return system_view_par(d, system_parity(d)); }
 
 // Launch helpers implemented in the kernel translation units.
 struct LaunchShape {
