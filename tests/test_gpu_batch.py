@@ -80,6 +80,26 @@ def test_mixed_batch_matches_standalone(gpu, method, precision, quad):
                 np.testing.assert_allclose(got[1], ref[1], rtol=0, atol=1e-5)
 
 
+def test_large_trees_match_standalone(gpu):
+    """Systems large enough for top levels: a batched tree builds at most 4
+    of them, a standalone 2^20-body tree 5; the cell numbering differs, the
+    trees and every result bit do not."""
+    nb = gpu
+    sizes = [1 << 20, 200000, 70000]
+    cfgs = [cfg(nb, n, True, quad=1) for n in sizes]
+    states = [(normal(n, 300 + k), lognormal_mass(n, 300 + k), small_vel(n, 300 + k)) for k, n in enumerate(sizes)]
+    dt, steps = 1e-3, 2
+    with nb.Batch(cfgs) as b:
+        for k, (p, m, v) in enumerate(states):
+            b.set_state(k, p, m, v)
+        b.step(dt, steps)
+        for k, (p, m, v) in enumerate(states):
+            got = b.get_state(k)
+            ref = standalone(nb, cfgs[k], p, m, v, dt, steps)
+            for a, r, what in zip(got[:3], ref[:3], ("pos", "vel", "acc")):
+                np.testing.assert_array_equal(a, r, err_msg=f"system {k} (n={sizes[k]}) {what}")
+
+
 def test_direct_systems_against_oracle(gpu, oracle):
     nb = gpu
     sizes = [257, 1000, 2048, 5]

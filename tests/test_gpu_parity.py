@@ -368,6 +368,40 @@ def test_tree_after_steps_equals_the_oracle(gpu, oracle):
     sim.close()
 
 
+@pytest.mark.parametrize("kind", ["ball", "normal"])
+def test_five_top_levels_equal_the_oracle(gpu, oracle, kind):
+    """At N = 2^20 the build first creates the cells of five top levels from
+    region counts (levels 1-4 in one block, level 5 over a grid) and starts
+    every insertion below them.  The tree in octant-path form, its cell
+    count and depth, the cell summaries and the sort still equal the
+    oracle's build bit for bit."""
+    nb = gpu
+    n = 1 << 20
+    pos = ball(n, 11) if kind == "ball" else normal(n, 11, (1.0, 1.0, 0.2))
+    mass = masses(n, 11, "equal" if kind == "ball" else "lognormal")
+    sim = bh_sim(nb, pos, mass, 0.5, 0.01)
+    sim.step(0.0, 1)
+    box = sim.stage_debug(nb.DEBUG_BBOX)
+    info = sim.stage_debug(nb.DEBUG_TREE_INFO)
+    cap = int(info[1])
+    t = oracle.tree_build(oracle.SEM_GEOMETRIC, pos, mass, box, cap)
+    assert t.status == 0
+    children = sim.stage_debug(nb.DEBUG_CHILDREN)
+    pg, dg, fg = oracle.tree_paths(children, n, n + cap)
+    po, do, fo = oracle.tree_paths(t.children, n, t.root)
+    assert fg == n and np.array_equal(pg, po) and np.array_equal(dg, do)
+    assert int(info[2]) == t.bottom and int(info[3]) == t.max_depth
+    octant_children = t.children.copy()
+    assert oracle.saturate(t) == 0
+    tg = cell_table(children, sim.stage_debug(nb.DEBUG_NODE_MASS), sim.stage_debug(nb.DEBUG_NODE_POS),
+                    sim.stage_debug(nb.DEBUG_BODY_COUNT), n, n + cap)
+    to = cell_table(octant_children, t.mass, t.pos, t.body_count, n, t.root)
+    assert tg == to
+    srt_o, _ = oracle.sort_bodies(t.children, n, t.root)
+    assert np.array_equal(sim.stage_debug(nb.DEBUG_SORTED), srt_o)
+    sim.close()
+
+
 def test_bounded_wait_gives_up_and_the_handle_recovers(gpu):
     """The timeout path, exercised without a hang: with the tree stages' wait
     cap at one iteration the sort's waits for parents give up, the step
