@@ -164,11 +164,12 @@ struct TopTables {
 constexpr int kTopMaxLevels = 5;                  // 8^5 = 32768 regions
 constexpr int kTopRegions = 1 << (3 * kTopMaxLevels);
 constexpr int kTopInner = (kTopRegions - 8) / 7;  // regions of levels 1..4: 8 + 64 + 512 + 4096
-// top levels for a tree of n bodies: about 32 bodies or more per region of the
-// deepest level, at most kTopMaxLevels, none below 2
+// top levels for a tree of n bodies: about 8 bodies or more per region of the
+// deepest level, at most kTopMaxLevels, none below 2 (262,144-body ball:
+// build 0.102 ms with 5 levels, 0.116 ms with 4)
 inline int top_levels_for(int n) {
     int l = 0;
-    while (l < kTopMaxLevels && (32LL << (3 * (l + 1))) <= (long long)n) ++l;
+    while (l < kTopMaxLevels && (8LL << (3 * (l + 1))) <= (long long)n) ++l;
     return l >= 2 ? l : 0;
 }
 // batched trees count in shared-memory bins per block of bodies, so at most
