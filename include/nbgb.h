@@ -165,9 +165,13 @@ nb_status nb_get_config(const nb_sim *sim, nb_config *out);
 /* ---- body state (the cl_p / cl_v / cl_m / cl_a buffers) ---- */
 /* Host arrays, reference layout.  vel3 may be NULL (zero velocities).
  * Resets the stored accelerations (InitObjectAcceleration,
- * src/MyApp.cpp:497-504).  n must equal num_of_bodies. */
+ * src/MyApp.cpp:497-504).  n must equal num_of_bodies.  Page-locked arrays
+ * (nb_host_alloc, cudaMallocHost, cudaHostRegister) are read by the device
+ * directly, without a staging copy; others are copied through a staging
+ * buffer. */
 nb_status nb_set_state(nb_sim *sim, const float *pos3, const float *vel3, const float *mass, int32_t n);
-/* Any output pointer may be NULL. */
+/* Any output pointer may be NULL.  Page-locked pos3 / vel3 (with acc3 and
+ * mass NULL) are written by the device directly. */
 nb_status nb_get_state(nb_sim *sim, float *pos3, float *vel3, float *acc3, float *mass);
 /* Seeded initial conditions of cfg (InitBodyAttributes, src/MyApp.cpp:331-495),
  * generated on the host.  Arrays: pos3/vel3 float[3N], mass float[N]. */
@@ -188,7 +192,8 @@ nb_status nb_step_async(nb_sim *sim, float dt, int32_t nsteps);
 nb_status nb_synchronize(nb_sim *sim);
 
 /* copy_vertices (kernels/copy_vertices.cl:3-17): float4{x,y,z,1} per body
- * into dst (device pointer if dst_is_device, else host). */
+ * into dst (device pointer if dst_is_device, 16-byte aligned; else host,
+ * written directly when page-locked and 16-byte aligned). */
 nb_status nb_copy_vertices(nb_sim *sim, float *dst4, int32_t dst_is_device);
 
 /* ---- introspection of the last step (parity and debugging) ---- */

@@ -280,11 +280,39 @@ nb_status nb_get_config(const nb_sim *s, nb_config *out) {
     return NB_OK;
 }
 
+// The device address of a host array the device can read and write
+// directly (page-locked: nb_host_alloc, cudaMallocHost, cudaHostRegister),
+// else null.  Such arrays are packed and unpacked by the kernels in place,
+// without a staging copy: one pass over the host link at full width.
+static void *host_device_view(const void *p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 nb_status nb_set_state(nb_sim *s, const float *pos3, const float *vel3, const float *mass, int32_t n) {
     if (!s || !pos3 || !mass) return fail(s, NB_ERR_INVALID_ARGUMENT, "nb_set_state: pos3 and mass are required");
     if (n != s->n) return fail(s, NB_ERR_INVALID_ARGUMENT, "nb_set_state: n differs from num_of_bodies");
     cudaSetDevice(s->dev);
     const size_t nn = (size_t)n;
+    {
+        const float *dp = static_cast<const float *>(host_device_view(pos3));
+        const float *dm = static_cast<const float *>(host_device_view(mass));
+        const float *dv = static_cast<const float *>(host_device_view(vel3));
+        if (dp && dm && (!vel3 || dv)) {  // page-locked: the kernel reads the host arrays
+            NB_CUDA(s, launch_pack(dp, dm, dv, s->body[s->cur], s->vel, s->acc, n, s->stream));
+            s->launches += 1;
+            NB_CUDA(s, cudaStreamSynchronize(s->stream));
+            s->have_state = true;
+            s->kdk_primed = false;
+            s->last_force_buf = -1;
+            return NB_OK;
+        }
+    }
     NB_CUDA(s, cudaMemcpyAsync(s->stage3, pos3, 12 * nn, cudaMemcpyHostToDevice, s->stream));
     NB_CUDA(s, cudaMemcpyAsync(s->stage1, mass, 4 * nn, cudaMemcpyHostToDevice, s->stream));
     float *dvel = nullptr;
@@ -322,6 +350,16 @@ nb_status nb_get_state(nb_sim *s, float *pos3, float *vel3, float *acc3, float *
     float *dv = reinterpret_cast<float *>(s->part);
     float *da = nullptr;  // acceleration staged behind the positions when asked
     std::vector<float> tmp;
+    if ((pos3 || vel3) && !acc3 && !mass) {
+        float *hp = static_cast<float *>(host_device_view(pos3));
+        float *hv = static_cast<float *>(host_device_view(vel3));
+        if ((!pos3 || hp) && (!vel3 || hv)) {  // page-locked: the kernel writes the host arrays
+            NB_CUDA(s, launch_unpack(s->body[s->cur], s->vel, s->acc, hp, hv, nullptr, s->n, s->stream));
+            s->launches += 1;
+            NB_CUDA(s, cudaStreamSynchronize(s->stream));
+            return NB_OK;
+        }
+    }
     if (pos3 || vel3) {
         NB_CUDA(s, launch_unpack(s->body[s->cur], s->vel, s->acc, pos3 ? s->stage3 : nullptr, vel3 ? dv : nullptr,
                                  nullptr, s->n, s->stream));
@@ -577,8 +615,13 @@ nb_status nb_copy_vertices(nb_sim *s, float *dst4, int32_t dst_is_device) {
     if (!s->have_state) return fail(s, NB_ERR_STATE, "nb_copy_vertices before nb_set_state");
     cudaSetDevice(s->dev);
     const size_t nn = (size_t)s->n;
+    const bool aligned = ((uintptr_t)dst4 & 15) == 0;  // float4 stores
     if (dst_is_device) {
+        if (!aligned) return fail(s, NB_ERR_INVALID_ARGUMENT, "nb_copy_vertices: a device dst must be 16-byte aligned");
         NB_CUDA(s, launch_copy_vertices(s->body[s->cur], s->n, reinterpret_cast<float4 *>(dst4), s->stream));
+        s->launches += 1;
+    } else if (float *hd = aligned ? static_cast<float *>(host_device_view(dst4)) : nullptr) {  // page-locked host
+        NB_CUDA(s, launch_copy_vertices(s->body[s->cur], s->n, reinterpret_cast<float4 *>(hd), s->stream));
         s->launches += 1;
     } else {
         NB_CUDA(s, launch_copy_vertices(s->body[s->cur], s->n, s->part, s->stream));

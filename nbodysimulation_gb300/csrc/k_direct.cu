@@ -326,36 +326,84 @@ __global__ void k_copy_vertices(const float4 *__restrict__ b, int n, float4 *__r
     }
 }
 
-__global__ void k_pack(const float *__restrict__ pos3, const float *__restrict__ mass, const float *__restrict__ vel3,
-                       float4 *body, float4 *vel, float4 *acc, int n) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (pos3) {
-            const float m = mass ? mass[i] : body[i].w;
-            body[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], m);
-        } else if (mass) {
-            body[i].w = mass[i];
+// The reference's packed float[3N] arrays <-> the float4 body layout.  A
+// block moves tiles of kPackTile bodies; when the float[3N] arrays are 16-byte
+// aligned, a whole tile's 3 * kPackTile floats move as contiguous float4
+// loads or stores through shared memory (the arrays may be pinned host
+// memory the device reads or writes directly, where full-width accesses
+// matter), otherwise as one float at a time.
+constexpr int kPackTile = 256;
+constexpr int kPackVec = kPackTile * 3 / 4;  // float4 per tile of float[3]
+
+__global__ void __launch_bounds__(kPackTile) k_pack(const float *__restrict__ pos3, const float *__restrict__ mass,
+                                                    const float *__restrict__ vel3, float4 *body, float4 *vel,
+                                                    float4 *acc, int n, int vec) {
+    __shared__ float4 tp[kPackVec], tv[kPackVec];
+    const float *fp = reinterpret_cast<const float *>(tp), *fv = reinterpret_cast<const float *>(tv);
+    const int t = threadIdx.x;
+    const int ntiles = (n + kPackTile - 1) / kPackTile;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const size_t i0 = (size_t)tile * kPackTile;
+        const size_t i = i0 + t;
+        const bool full = vec && i0 + kPackTile <= (size_t)n;  // block-uniform
+        if (full && t < kPackVec) {
+            if (pos3) tp[t] = reinterpret_cast<const float4 *>(pos3 + 3 * i0)[t];
+            if (vel3) tv[t] = reinterpret_cast<const float4 *>(vel3 + 3 * i0)[t];
         }
-        if (vel) vel[i] = vel3 ? make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0f)
-                               : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (acc) acc[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        __syncthreads();
+        if (i < (size_t)n) {
+            if (pos3) {
+                const float m = mass ? mass[i] : body[i].w;
+                body[i] = full ? make_float4(fp[3 * t], fp[3 * t + 1], fp[3 * t + 2], m)
+                               : make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], m);
+            } else if (mass) {
+                body[i].w = mass[i];
+            }
+            if (vel) {
+                float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (vel3) v = full ? make_float4(fv[3 * t], fv[3 * t + 1], fv[3 * t + 2], 0.0f)
+                                   : make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0f);
+                vel[i] = v;
+            }
+            if (acc) acc[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        __syncthreads();  // the tile is read before the next one is staged
     }
 }
 
-__global__ void k_unpack(const float4 *__restrict__ body, const float4 *__restrict__ vel,
-                         const float4 *__restrict__ acc, float *pos3, float *vel3, float *acc3, int n) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (pos3) {
-            const float4 p = body[i];
-            pos3[3 * i] = p.x; pos3[3 * i + 1] = p.y; pos3[3 * i + 2] = p.z;
-        }
-        if (vel3) {
-            const float4 v = vel[i];
-            vel3[3 * i] = v.x; vel3[3 * i + 1] = v.y; vel3[3 * i + 2] = v.z;
-        }
-        if (acc3) {
-            const float4 a = acc[i];
-            acc3[3 * i] = a.x; acc3[3 * i + 1] = a.y; acc3[3 * i + 2] = a.z;
-        }
+// one float4 array -> one float[3N] array, tile at i0 (block-uniform `full`)
+__device__ __forceinline__ void unpack_tile(const float4 *__restrict__ src, float *dst, size_t i0, int n, bool full,
+                                            float4 *tile) {
+    const int t = threadIdx.x;
+    const size_t i = i0 + t;
+    if (full) {
+        float *f = reinterpret_cast<float *>(tile);
+        const float4 v = src[i];
+        f[3 * t] = v.x;
+        f[3 * t + 1] = v.y;
+        f[3 * t + 2] = v.z;
+        __syncthreads();
+        if (t < kPackVec) reinterpret_cast<float4 *>(dst + 3 * i0)[t] = tile[t];
+        __syncthreads();
+    } else if (i < (size_t)n) {
+        const float4 v = src[i];
+        dst[3 * i] = v.x;
+        dst[3 * i + 1] = v.y;
+        dst[3 * i + 2] = v.z;
+    }
+}
+
+__global__ void __launch_bounds__(kPackTile) k_unpack(const float4 *__restrict__ body, const float4 *__restrict__ vel,
+                                                      const float4 *__restrict__ acc, float *pos3, float *vel3,
+                                                      float *acc3, int n, int vec) {
+    __shared__ float4 tile[kPackVec];
+    const int ntiles = (n + kPackTile - 1) / kPackTile;
+    for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
+        const size_t i0 = (size_t)k * kPackTile;
+        const bool full = vec && i0 + kPackTile <= (size_t)n;  // block-uniform
+        if (pos3) unpack_tile(body, pos3, i0, n, full, tile);
+        if (vel3) unpack_tile(vel, vel3, i0, n, full, tile);
+        if (acc3) unpack_tile(acc, acc3, i0, n, full, tile);
     }
 }
 
@@ -444,17 +492,23 @@ cudaError_t launch_copy_vertices(const float4 *body, int n, float4 *dst, cudaStr
     return cudaGetLastError();
 }
 
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
 cudaError_t launch_pack(const float *pos3, const float *mass, const float *vel3, float4 *body, float4 *vel,
                         float4 *acc, int n, cudaStream_t st) {
-    const int blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
-    k_pack<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(pos3, mass, vel3, body, vel, acc, n);
+    const int tiles = (n + kPackTile - 1) / kPackTile;
+    const int blocks = tiles < 4096 ? tiles : 4096;
+    const int vec = aligned16(pos3) && aligned16(vel3);
+    k_pack<<<blocks > 0 ? blocks : 1, kPackTile, 0, st>>>(pos3, mass, vel3, body, vel, acc, n, vec);
     return cudaGetLastError();
 }
 
 cudaError_t launch_unpack(const float4 *body, const float4 *vel, const float4 *acc, float *pos3, float *vel3,
                           float *acc3, int n, cudaStream_t st) {
-    const int blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
-    k_unpack<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(body, vel, acc, pos3, vel3, acc3, n);
+    const int tiles = (n + kPackTile - 1) / kPackTile;
+    const int blocks = tiles < 4096 ? tiles : 4096;
+    const int vec = aligned16(pos3) && aligned16(vel3) && aligned16(acc3);
+    k_unpack<<<blocks > 0 ? blocks : 1, kPackTile, 0, st>>>(body, vel, acc, pos3, vel3, acc3, n, vec);
     return cudaGetLastError();
 }
 

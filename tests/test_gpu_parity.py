@@ -280,6 +280,46 @@ def test_copy_vertices(gpu, oracle):
     assert np.array_equal(sim.copy_vertices(), oracle.copy_vertices(pos))
 
 
+@pytest.mark.parametrize("n,offset", [(1000, 0), (70000, 0), (70000, 4), (256 * 40, 8)])
+def test_page_locked_host_arrays(gpu, oracle, n, offset):
+    """Page-locked host arrays are packed and unpacked by the device in
+    place (float4 tiles when 16-byte aligned, single floats otherwise); the
+    state and the vertices equal those of ordinary host arrays bit for bit."""
+    import ctypes
+    nb = gpu
+    L = nb.load()
+    pos, mass = normal(n, 21), masses(n, 21, "lognormal")
+    vel = (0.1 * normal(n, 22)).astype(np.float32)
+    plain = bh_sim(nb, pos, mass, 0.5, 0.01, vel=vel)
+    plain.step(1e-3, 2)
+    want = plain.get_state()
+    want_v = plain.copy_vertices()
+    plain.close()
+
+    sizes = (12 * n, 12 * n, 4 * n, 12 * n, 12 * n, 16 * n)
+    bufs = [L.nb_host_alloc(b + offset) for b in sizes]
+    assert all(bufs)
+    try:
+        arr = [np.ctypeslib.as_array((ctypes.c_float * (b // 4)).from_address(p + offset)) for p, b in zip(bufs, sizes)]
+        arr[0][:] = pos.ravel()
+        arr[1][:] = vel.ravel()
+        arr[2][:] = mass
+        # another state first, so that the page-locked one must replace it
+        sim = bh_sim(nb, normal(n, 99), masses(n, 99), 0.5, 0.01)
+        addr = [p + offset for p in bufs]
+        assert L.nb_set_state(sim.h, addr[0], addr[1], addr[2], n) == 0
+        sim.step(1e-3, 2)
+        assert L.nb_get_state(sim.h, addr[3], addr[4], None, None) == 0
+        np.testing.assert_array_equal(arr[3].reshape(n, 3), want[0])
+        np.testing.assert_array_equal(arr[4].reshape(n, 3), want[1])
+        assert L.nb_copy_vertices(sim.h, addr[5], 0) == 0
+        np.testing.assert_array_equal(arr[5].reshape(n, 4), want_v)
+        sim.close()
+    finally:
+        for p in bufs:
+            L.nb_host_free(p)
+
+
 def test_compensated_accumulation(gpu, oracle):
     nb = gpu
     n = 20000
