@@ -183,23 +183,26 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
                 ++n_cell;
                 const float r = rsqrt_fast(d2);
                 const float r2 = r * r;
-                const float r3 = r * r2;
-                float F = q.w * r3;
-                if constexpr (kQuad) {  // + 2.5 (d.Q.d) d / r^7 - Q d / r^5
+                if constexpr (kQuad) {
+                    // m d / r^3 + 2.5 (d.Q.d) d / r^7 - Q d / r^5
+                    //   = (d (m d^2 + 2.5 (d.Q.d) / r^2) - Q d) / r^5, with r^-2 = d^2:
+                    // 24 FP32 operations instead of 26
                     const float4 Q = cqa[k];  // xx yy zz xy; mt.x = xz, mt.y = yz
                     const float qx = fmaf(mt.x, dz, fmaf(Q.w, dy, Q.x * dx));
                     const float qy = fmaf(mt.y, dz, fmaf(Q.y, dy, Q.w * dx));
                     const float qz = fmaf(Q.z, dz, fmaf(mt.y, dy, mt.x * dx));
                     const float sq = fmaf(dz, qz, fmaf(dy, qy, dx * qx));
-                    const float r5 = r3 * r2;
-                    F = fmaf(2.5f * sq, r5 * r2, F);
-                    sx = fmaf(-qx, r5, sx);
-                    sy = fmaf(-qy, r5, sy);
-                    sz = fmaf(-qz, r5, sz);
+                    const float r5 = r * (r2 * r2);
+                    const float t = fmaf(2.5f * sq, r2, q.w * d2);
+                    sx = fmaf(fmaf(dx, t, -qx), r5, sx);
+                    sy = fmaf(fmaf(dy, t, -qy), r5, sy);
+                    sz = fmaf(fmaf(dz, t, -qz), r5, sz);
+                } else {
+                    const float F = q.w * (r * r2);
+                    sx = fmaf(dx, F, sx);
+                    sy = fmaf(dy, F, sy);
+                    sz = fmaf(dz, F, sz);
                 }
-                sx = fmaf(dx, F, sx);
-                sy = fmaf(dy, F, sy);
-                sz = fmaf(dz, F, sz);
             } else if (sp < kStack) {
                 if (lane == 0) stack[sp] = __float_as_int(mt.w);
                 ++sp;
