@@ -173,14 +173,15 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
             sy = fmaf(dy, F, sy);
             sz = fmaf(dz, F, sz);
         }
-        // child cells: accumulated when every lane accepts, else pushed
+        // child cells: accumulated when every lane accepts, else pushed (and
+        // taken off the count of cell interactions, which is rarer than adding)
+        n_cell += nc;
         for (int k = 0; k < nc; ++k) {
             const float4 q = cpm[k];
             const float4 mt = cmeta[k];
             const float dx = q.x - P.x, dy = q.y - P.y, dz = q.z - P.z;
             const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
             if (__all_sync(0xffffffffu, d2 >= mt.z)) {
-                ++n_cell;
                 const float r = rsqrt_fast(d2);
                 const float r2 = r * r;
                 if constexpr (kQuad) {
@@ -206,8 +207,10 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
             } else if (sp < kStack) {
                 if (lane == 0) stack[sp] = __float_as_int(mt.w);
                 ++sp;
-            } else if (lane == 0) {  // outside the stack bound: never overrun shared memory
-                set_status(ctrl, kStDepth, kStack);
+                --n_cell;
+            } else {  // outside the stack bound: never overrun shared memory
+                --n_cell;
+                if (lane == 0) set_status(ctrl, kStDepth, kStack);
             }
         }
         if constexpr (kComp) {  // one TwoSum per batch into the running sum
