@@ -284,14 +284,16 @@ nb_status nb_get_config(const nb_sim *s, nb_config *out) {
 // directly (page-locked: nb_host_alloc, cudaMallocHost, cudaHostRegister),
 // else null.  Such arrays are packed and unpacked by the kernels in place,
 // without a staging copy: one pass over the host link at full width.
-static void *host_device_view(const void *p) {
+static void *host_device_view(const void *p, int dev) {
     if (!p) return nullptr;
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    // page-locked for this handle's device (allocated or registered while it
+    // was current); other arrays take the staging copy
+    return a.type == cudaMemoryTypeHost && a.device == dev ? a.devicePointer : nullptr;
 }
 
 nb_status nb_set_state(nb_sim *s, const float *pos3, const float *vel3, const float *mass, int32_t n) {
@@ -300,9 +302,9 @@ nb_status nb_set_state(nb_sim *s, const float *pos3, const float *vel3, const fl
     cudaSetDevice(s->dev);
     const size_t nn = (size_t)n;
     {
-        const float *dp = static_cast<const float *>(host_device_view(pos3));
-        const float *dm = static_cast<const float *>(host_device_view(mass));
-        const float *dv = static_cast<const float *>(host_device_view(vel3));
+        const float *dp = static_cast<const float *>(host_device_view(pos3, s->dev));
+        const float *dm = static_cast<const float *>(host_device_view(mass, s->dev));
+        const float *dv = static_cast<const float *>(host_device_view(vel3, s->dev));
         if (dp && dm && (!vel3 || dv)) {  // page-locked: the kernel reads the host arrays
             NB_CUDA(s, launch_pack(dp, dm, dv, s->body[s->cur], s->vel, s->acc, n, s->stream));
             s->launches += 1;
@@ -351,8 +353,8 @@ nb_status nb_get_state(nb_sim *s, float *pos3, float *vel3, float *acc3, float *
     float *da = nullptr;  // acceleration staged behind the positions when asked
     std::vector<float> tmp;
     if ((pos3 || vel3) && !acc3 && !mass) {
-        float *hp = static_cast<float *>(host_device_view(pos3));
-        float *hv = static_cast<float *>(host_device_view(vel3));
+        float *hp = static_cast<float *>(host_device_view(pos3, s->dev));
+        float *hv = static_cast<float *>(host_device_view(vel3, s->dev));
         if ((!pos3 || hp) && (!vel3 || hv)) {  // page-locked: the kernel writes the host arrays
             NB_CUDA(s, launch_unpack(s->body[s->cur], s->vel, s->acc, hp, hv, nullptr, s->n, s->stream));
             s->launches += 1;
@@ -620,7 +622,7 @@ nb_status nb_copy_vertices(nb_sim *s, float *dst4, int32_t dst_is_device) {
         if (!aligned) return fail(s, NB_ERR_INVALID_ARGUMENT, "nb_copy_vertices: a device dst must be 16-byte aligned");
         NB_CUDA(s, launch_copy_vertices(s->body[s->cur], s->n, reinterpret_cast<float4 *>(dst4), s->stream));
         s->launches += 1;
-    } else if (float *hd = aligned ? static_cast<float *>(host_device_view(dst4)) : nullptr) {  // page-locked host
+    } else if (float *hd = aligned ? static_cast<float *>(host_device_view(dst4, s->dev)) : nullptr) {  // page-locked host
         NB_CUDA(s, launch_copy_vertices(s->body[s->cur], s->n, reinterpret_cast<float4 *>(hd), s->stream));
         s->launches += 1;
     } else {
