@@ -57,7 +57,7 @@ PROBE_SAMPLES = 8192
 FP32_LANES_PER_SM = 128
 MUFU_LANES_PER_SM = 16  # rsqrt results per SM per clock
 FLOPS_PER_INTERACTION = 12  # FP32 ops per monopole interaction (3 sub, 3 fma, 3 mul, 3 fma)
-FORCE_DRAM_BYTES_PER_BODY = (387.995392e6 + 75.690752e6) / 1048576  # dram read + write, k_force, N = 1M
+FORCE_DRAM_BYTES_PER_BODY = (390.426624e6 + 75.037696e6) / 1048576  # dram read + write, k_force, N = 1M
 FLOPS_PER_QUADRUPOLE = 19   # extra FP32 ops per cell quadrupole term (Q.d 9, d.Q.d 3, r^5 r^7 2, 2.5*sq 1, 4 fma)
 
 
