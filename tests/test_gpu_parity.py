@@ -320,6 +320,52 @@ def test_page_locked_host_arrays(gpu, oracle, n, offset):
             L.nb_host_free(p)
 
 
+def test_known_answer_sets(gpu, oracle):
+    """The hand-built sets of the oracle's known-answer tests
+    (test_oracle_analytic.py) through the C ABI: two-body forces against the
+    closed form, the nine-body centre at rest to rounding, the root of one
+    body per octant and the tree of two bodies that separate at depth 10."""
+    import test_oracle_analytic as K
+    nb = gpu
+
+    def accel(pos, mass, algo, eps, G, theta=0.5):
+        with nb.Simulation(num_of_bodies=len(mass), algo_config=algo, theta=theta, epsilon=eps,
+                           gravitational_constant=G) as sim:
+            sim.set_state(pos, mass)
+            sim.step(0.0, 1)
+            return sim.get_state()[2]
+
+    pos, mass = K.two_bodies()
+    want = K.analytic_two_body(pos, mass, float(np.float32(0.05)), 1.5)
+    for algo in (nb.BRUTE_FORCE_GLOBAL, nb.BRUTE_FORCE_LOCAL, nb.BARNES_HUT):
+        np.testing.assert_allclose(accel(pos, mass, algo, 0.05, 1.5), want, rtol=2e-6, atol=0, err_msg=str(algo))
+
+    pos, mass = K.nine_bodies()
+    for algo in (nb.BRUTE_FORCE_GLOBAL, nb.BRUTE_FORCE_LOCAL, nb.BARNES_HUT):
+        acc = accel(pos, mass, algo, 0.01, 1.0, theta=0.0)
+        assert np.max(np.abs(acc[8])) <= 8 * 3.0 ** -1.5 * 4 * 2.0 ** -23, (algo, acc[8])
+        assert np.all(np.sign(acc[:8]) == -np.sign(pos[:8])), algo
+
+    pos, mass = K.one_per_octant()
+    with bh_sim(nb, pos, mass, 0.5, 0.01) as sim:
+        sim.step(0.0, 1)
+        info = sim.stage_debug(nb.DEBUG_TREE_INFO)
+        cap = int(info[1])
+        root_row = sim.stage_debug(nb.DEBUG_CHILDREN).reshape(-1, 8)[8 + cap]
+        assert int(info[2]) == 8 + cap  # no cell
+        assert [K.slot_of(pos[b]) for b in root_row] == list(range(8))
+
+    pos, mass = K.chain_bodies()
+    with bh_sim(nb, pos, mass, 0.5, 0.01) as sim:
+        sim.step(0.0, 1)
+        info = sim.stage_debug(nb.DEBUG_TREE_INFO)
+        cap = int(info[1])
+        assert 4 + cap - int(info[2]) == 10 and int(info[3]) == 10
+        paths, depth, found = oracle.tree_paths(sim.stage_debug(nb.DEBUG_CHILDREN), 4, 4 + cap)
+        a, b = K.chain_expected()
+        assert found == 4 and list(paths[2, :depth[2]]) == a and list(paths[3, :depth[3]]) == b
+
+
 def test_compensated_accumulation(gpu, oracle):
     nb = gpu
     n = 20000
