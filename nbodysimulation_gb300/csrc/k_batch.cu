@@ -505,7 +505,9 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
         k_batch_top_cells<<<t.nsys, 256, 0, st>>>(t);
         k_batch_build<<<t.chunks, 256, 0, st>>>(t);
         k_batch_used<<<1, kScanThreads, 0, st>>>(t);
-        int sblocks = sm_count * 8;
+        // many blocks, so the grid-stride tail is short (512 systems: 8 per SM
+        // 4.79 ms, 32 per SM 2.90 ms)
+        int sblocks = sm_count * 32;
         const int need = (t.cells + 255) / 256;
         if (sblocks > need) sblocks = need;
         if (quad) k_batch_summarize<true><<<sblocks, 256, 0, st>>>(t);
