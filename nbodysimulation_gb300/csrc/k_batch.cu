@@ -274,21 +274,21 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
     // its kernel parameters, instead of holding them in registers
     __shared__ DevSim s_view[kForceWarps];
     __shared__ StepParams s_par[kForceWarps];
+    // the current system of each warp, its first group and its mode (0 walk,
+    // 1 keep the step-start state of a failed step, 2 inert): in shared
+    // memory, so nothing of the outer loop stays live in registers during a walk
+    __shared__ int s_cur[kForceWarps], s_begin[kForceWarps], s_mode[kForceWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const WarpStage ws{s_stack[w], s_bpm[w], s_cpm[w], s_cmeta[w], s_cqa[w]};
-    float *dq = s_dq[w];
-    int cur = -1, begin = 0;
-    int mode = 0;  // 0 walk, 1 keep the step-start state (failed step), 2 inert
+    if (lane == 0) s_cur[w] = -1;
+    __syncwarp();
     while (true) {
         int gg = 0;
         if (lane == 0) gg = atomicAdd(t.work, 1);
         gg = __shfl_sync(0xffffffffu, gg, 0);
         if (gg >= t.groups) break;
         const int k = find_system(t.group_prefix, t.nsys, gg);
-        if (k != cur) {
-            cur = k;
+        if (k != s_cur[w]) {
             __syncwarp();  // the previous system's view and thresholds are no longer read
-            int sk = 0;
             if (lane == 0) {
                 const SysDesc &d = t.sys[k];
                 const DevSim v = system_view(d);
@@ -296,6 +296,7 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
                 p.kdk_primed = v.ctrl->kdk_primed;
                 s_view[w] = v;
                 s_par[w] = p;
+                int sk = 0;
                 if (!system_live(v.ctrl)) {
                     sk = 2;
                 } else if (read_status(v.ctrl)) {
@@ -306,14 +307,15 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
                 }
                 float box[6];
                 load_box(v.ctrl, box);
-                make_thresholds(box, p.theta, p.eps, p.crit_ref, dq);
-                begin = d.group_begin;
+                make_thresholds(box, p.theta, p.eps, p.crit_ref, s_dq[w]);
+                s_cur[w] = k;
+                s_begin[w] = d.group_begin;
+                s_mode[w] = sk;
             }
-            mode = __shfl_sync(0xffffffffu, sk, 0);
-            begin = __shfl_sync(0xffffffffu, begin, 0);
             __syncwarp();
         }
-        const int g = gg - begin;
+        const int g = gg - s_begin[w];
+        const int mode = s_mode[w];
         const DevSim &s = s_view[w];
         if (mode == 2) continue;
         if (mode == 1) {  // keep the step-start state
@@ -321,7 +323,8 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
             if (i < s.n) s.body_next[i] = s.body_cur[i];
             continue;
         }
-        force_group<kMethod, kComp, false, kQuad>(s, s_par[w], dq, g, lane, ws);
+        const WarpStage ws{s_stack[w], s_bpm[w], s_cpm[w], s_cmeta[w], s_cqa[w]};
+        force_group<kMethod, kComp, false, kQuad>(s, s_par[w], s_dq[w], g, lane, ws);
     }
 }
 
