@@ -44,6 +44,7 @@ struct nb_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    StepFork fork{};  // the captured step's second branch (direct sums)
     long long launches = 0;
     int launches_per_step = 0;
     nb_status last = NB_OK;
@@ -166,7 +167,11 @@ nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out) {
     };
     if (cudaSetDevice(b->dev) != cudaSuccess) return fail_all(NB_ERR_CUDA);
     cudaDeviceGetAttribute(&b->sm, cudaDevAttrMultiProcessorCount, b->dev);
-    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) return fail_all(NB_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->fork.aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork.join, cudaEventDisableTiming) != cudaSuccess)
+        return fail_all(NB_ERR_CUDA);
     b->mem.resize(nsys);
     size_t total = 0;
     int maxn = 0;
@@ -237,6 +242,9 @@ nb_status nb_batch_destroy(nb_batch *b) {
     cudaFree(b->d_stage);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
+    if (b->fork.fork) cudaEventDestroy(b->fork.fork);
+    if (b->fork.join) cudaEventDestroy(b->fork.join);
+    if (b->fork.aux) cudaStreamDestroy(b->fork.aux);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
     return NB_OK;
@@ -326,7 +334,7 @@ static nb_status enqueue_steps(nb_batch *b, float dt, int nsteps) {
         // the device, so the same graph serves every step
         B_CUDA(b, cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
         int nl = 0;
-        cudaError_t e = launch_batch_step(b->t, b->method, b->comp, b->quad, b->variant, b->sm, b->st, &nl);
+        cudaError_t e = launch_batch_step(b->t, b->method, b->comp, b->quad, b->variant, b->sm, b->st, &b->fork, &nl);
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(b->st, &g);
         if (e != cudaSuccess || e2 != cudaSuccess) {

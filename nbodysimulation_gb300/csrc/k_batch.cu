@@ -497,10 +497,19 @@ static cudaError_t launch_batch_force_m(const BatchTables &t, int comp, int quad
 // One batched step.  Kernels with no work in this batch are not launched.
 // Returns the number of kernels launched through *launches.
 cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int quad, int direct_variant,
-                              int sm_count, cudaStream_t st, int *launches) {
+                              int sm_count, cudaStream_t st, const StepFork *fork, int *launches) {
     int nl = 0;
     cudaError_t e = cudaSuccess;
     const int sb = (t.nsys + 127) / 128;
+    const bool branch = fork && fork->aux && t.chunks > 0 && t.dblocks > 0;
+    if (branch) {  // the direct sum beside the tree stages
+        if ((e = cudaEventRecord(fork->fork, st)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(fork->aux, fork->fork, 0)) != cudaSuccess ||
+            (e = launch_direct_variant(t, direct_variant, fork->aux)) != cudaSuccess ||
+            (e = cudaEventRecord(fork->join, fork->aux)) != cudaSuccess)
+            return e;
+        nl += 1;
+    }
     if (t.chunks > 0) {
         k_batch_reset<<<sb, 128, 0, st>>>(t);
         k_batch_bbox<<<t.chunks, 256, 0, st>>>(t);
@@ -515,6 +524,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
         if (sblocks > need) sblocks = need;
         if (quad) k_batch_summarize<true><<<sblocks, 256, 0, st>>>(t);
         else k_batch_summarize<false><<<sblocks, 256, 0, st>>>(t);
+        if (branch && (e = cudaStreamWaitEvent(st, fork->join, 0)) != cudaSuccess) return e;
         int rblocks = resident((const void *)k_batch_sort, 256, sm_count);
         if (rblocks > need) rblocks = need;
         k_batch_sort<<<rblocks, 256, 0, st>>>(t);
@@ -528,7 +538,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
         if (e != cudaSuccess) return e;
         nl += 9;
     }
-    if (t.dblocks > 0) {
+    if (t.dblocks > 0 && !branch) {
         if ((e = launch_direct_variant(t, direct_variant, st)) != cudaSuccess) return e;
         nl += 1;
     }

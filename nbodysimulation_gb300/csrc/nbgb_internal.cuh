@@ -272,8 +272,16 @@ inline int batch_chunk(int n, long long batch_tree_bodies) {
 }
 int batch_direct_variants();
 int batch_direct_block_bodies(int variant);
+// Optional second stream of a captured batched step: the small systems'
+// direct sum runs on it beside the tree stages up to the summarisation (a
+// parallel branch of the graph); the sort, whose waits assume its whole grid
+// is resident, starts after both.
+struct StepFork {
+    cudaStream_t aux;
+    cudaEvent_t fork, join;
+};
 cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int quad, int direct_variant,
-                              int sm_count, cudaStream_t st, int *launches);
+                              int sm_count, cudaStream_t st, const StepFork *fork, int *launches);
 cudaError_t launch_batch_direct_only(const BatchTables &t, int variant, cudaStream_t st);
 // clears the status word and work counters of every system (once per call)
 cudaError_t launch_batch_clear(const BatchTables &t, cudaStream_t st);

@@ -80,6 +80,7 @@ struct nb_server {
     void *user = nullptr;
     int dev = 0, sm = 0, variant = 3;
     cudaStream_t compute = nullptr, upload = nullptr, out = nullptr, cap = nullptr;
+    StepFork fork{};  // the captured round step's second branch (direct sums)
     Admission adm{0, 0};
     Clock::time_point t0;
 
@@ -306,7 +307,7 @@ static cudaError_t launch_round(nb_server *s, std::vector<JobP> &run, int steps,
         const int quad = s->cfg.multipole == NB_MULTIPOLE_QUADRUPOLE;
         if ((e = cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
         int nl = 0;
-        cudaError_t le = launch_batch_step(t, method, comp, quad, s->variant, s->sm, s->cap, &nl);
+        cudaError_t le = launch_batch_step(t, method, comp, quad, s->variant, s->sm, s->cap, &s->fork, &nl);
         cudaGraph_t g = nullptr;
         e = cudaStreamEndCapture(s->cap, &g);
         if (le != cudaSuccess) e = le;
@@ -551,6 +552,9 @@ nb_status nb_server_create(const nb_server_config *c, nb_job_fn fn, void *user, 
               cudaStreamCreateWithFlags(&s->upload, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->out, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&s->fork.aux, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->fork.fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->fork.join, cudaEventDisableTiming) == cudaSuccess &&
               cudaMalloc(&s->d_work, sizeof(int)) == cudaSuccess;
     for (int b = 0; b < 2 && ok; ++b) {
         ok = cudaMalloc(&s->d_sys[b], sizeof(SysDesc) * ns) == cudaSuccess &&
@@ -729,7 +733,9 @@ nb_status nb_server_destroy(nb_server *s) {
         if (s->round_ev[b]) cudaEventDestroy(s->round_ev[b]);
     }
     cudaFree(s->d_work);
-    for (cudaStream_t st : {s->compute, s->upload, s->out, s->cap})
+    if (s->fork.fork) cudaEventDestroy(s->fork.fork);
+    if (s->fork.join) cudaEventDestroy(s->fork.join);
+    for (cudaStream_t st : {s->compute, s->upload, s->out, s->cap, s->fork.aux})
         if (st) cudaStreamDestroy(st);
     delete s;
     return NB_OK;
