@@ -12,7 +12,8 @@ accumulation, seeded synthetic data.  Metric: body-updates/s.
 `value` is device time (CUDA events on the library's stream) with the bodies
 resident in HBM; `e2e` goes through the public C ABI every step:
 nb_set_state from pinned host arrays, nb_step, nb_get_state into pinned host
-arrays.  The accuracy gate (RMS relative force error vs an FP64 direct sum
+arrays (page-locked: the library's kernels read and write them across the host
+link in place, with no staging copy).  The accuracy gate (RMS relative force error vs an FP64 direct sum
 on 8192 sample bodies <= 1e-3) is evaluated after the timed region.
 
 The same line carries more measurements, each with its own timed region
