@@ -7,7 +7,6 @@
 // (kernels/sort.cl).  Each is re-designed for sm_103a; the differences that
 // change results are listed at each kernel.
 #include <algorithm>
-#include <atomic>
 
 #include "bh_device.cuh"
 
@@ -210,17 +209,10 @@ cudaError_t launch_build(const DevSim &s, const TopTables &top, int tree_ref, in
     const int need = (s.n + 255) / 256;
     if (!tree_ref && top.levels >= 2 && top.levels <= kTopMaxLevels) {
         const size_t bins_bytes = sizeof(int) << (3 * top.levels);
-        // the 8^5-bin table needs the opt-in shared memory size, set once per device
-        static std::atomic<unsigned long long> bins_attr{0};
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e != cudaSuccess) return e;
-        const unsigned long long bit = 1ull << (dev & 63);
-        if (!(bins_attr.load() & bit)) {
-            e = cudaFuncSetAttribute(k_top_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(sizeof(int) * kTopRegions));
+        if (bins_bytes > 48 * 1024) {  // the 8^5-bin table needs the opt-in shared memory size (current device)
+            const cudaError_t e = cudaFuncSetAttribute(k_top_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)bins_bytes);
             if (e != cudaSuccess) return e;
-            bins_attr.fetch_or(bit);
         }
         const int cblocks = std::max(1, std::min(sm_count, (s.n + kTopCountThreads - 1) / kTopCountThreads));
         k_top_count<<<cblocks, kTopCountThreads, bins_bytes, st>>>(s, top);
