@@ -100,6 +100,32 @@ def test_large_trees_match_standalone(gpu):
                 np.testing.assert_array_equal(a, r, err_msg=f"system {k} (n={sizes[k]}) {what}")
 
 
+def test_reference_tree_semantics_match_standalone(gpu):
+    """Batched trees with the reference's tree and opening semantics (the
+    insertions start at the root; no top levels) against standalone handles
+    with the same settings, bit for bit, beside a default-semantics tree."""
+    nb = gpu
+    sizes = [(30000, 1), (50000, 0), (9001, 1)]
+    cfgs = []
+    for n, ref in sizes:
+        c = cfg(nb, n, True)
+        c.tree_semantics = ref
+        c.theta_semantics = ref
+        cfgs.append(c)
+    states = [(normal(n, 500 + k), lognormal_mass(n, 500 + k), small_vel(n, 500 + k))
+              for k, (n, _) in enumerate(sizes)]
+    dt, steps = 1e-3, 3
+    with nb.Batch(cfgs) as b:
+        for k, (p, m, v) in enumerate(states):
+            b.set_state(k, p, m, v)
+        b.step(dt, steps)
+        for k, (p, m, v) in enumerate(states):
+            got = b.get_state(k)
+            ref = standalone(nb, cfgs[k], p, m, v, dt, steps)
+            for a, r, what in zip(got[:3], ref[:3], ("pos", "vel", "acc")):
+                np.testing.assert_array_equal(a, r, err_msg=f"system {k} {what}")
+
+
 def test_direct_systems_against_oracle(gpu, oracle):
     nb = gpu
     sizes = [257, 1000, 2048, 5]
