@@ -434,10 +434,23 @@ static cudaError_t launch_direct_t(const DevSim &s, const StepParams &p, float e
     // over gridDim.y
     const int want = sm_count * 6;
     const int bx4 = (n + kTiledThreads * 4 - 1) / (kTiledThreads * 4);
+    const int bx3 = (n + kTiledThreads * 3 - 1) / (kTiledThreads * 3);
     const int bx2 = (n + kTiledThreads * 2 - 1) / (kTiledThreads * 2);
     const int bx1 = (n + kTiledThreads - 1) / kTiledThreads;
     const int ntiles = (n + kTile - 1) / kTile;
     if (bx4 >= want) {
+        // every block does the same work, so the busiest SM holds
+        // ceil(blocks / SMs) of them: 3 targets per thread when that evens
+        // the SMs out enough to pay for the extra shared-memory load per pair
+        // (N = 262,144: 1024 blocks of 4 -> 7 on the busiest SM, 28 target
+        // rows; 1366 blocks of 3 -> 9, 27)
+        const long long cost4 = 4LL * ((bx4 + sm_count - 1) / sm_count);
+        const long long cost3 = 3LL * ((bx3 + sm_count - 1) / sm_count);
+        if (cost3 < cost4) {
+            k_direct_tiled<3, 2, kMethod, kQuirk, kEpsZero><<<dim3(bx3, 1), 2 * kTiledThreads, 0, st>>>(s, p, eps,
+                                                                                                     part);
+            return cudaGetLastError();
+        }
         k_direct_tiled<4, 2, kMethod, kQuirk, kEpsZero><<<dim3(bx4, 1), 2 * kTiledThreads, 0, st>>>(s, p, eps, part);
         return cudaGetLastError();
     }
