@@ -33,7 +33,8 @@ The same line carries more measurements, each with its own timed region
 Under torchrun (--gpus N > 1) every rank advances its own independent
 system on its own GPU (replicas; no exchange); rank 0 prints the aggregate.
 --impl reference times the CPU restatement of the reference's kernels
-(oracle/, OpenMP) on a bounded sample of the same workload.
+(oracle/, OpenMP on every host thread): whole steps of all N bodies of the
+same workload, without loading the GPU library.
 """
 from __future__ import annotations
 
@@ -57,9 +58,19 @@ WORKLOAD = dict(name="bh_plummer_n4m_theta0.5", n=4194304, sigma=(1.0, 1.0, 0.2)
 PROBE_SAMPLES = 8192
 FP32_LANES_PER_SM = 128
 MUFU_LANES_PER_SM = 16  # rsqrt results per SM per clock
-FLOPS_PER_INTERACTION = 12  # FP32 ops per monopole interaction (3 sub, 3 fma, 3 mul, 3 fma)
-FORCE_DRAM_BYTES_PER_BODY = (390.426624e6 + 75.037696e6) / 1048576  # dram read + write, k_force, N = 1M
-FLOPS_PER_QUADRUPOLE = 19   # extra FP32 ops per cell quadrupole term (Q.d 9, d.Q.d 3, r^5 r^7 2, 2.5*sq 1, 4 fma)
+# FP32-pipe operations of the force walk's arithmetic, counted in its source:
+# a body (or monopole cell) interaction is d = x_j - x_i (3 FADD), d^2 + eps^2
+# (3 FFMA), F = m r^3 (3 FMUL), a += d F (3 FFMA) = 12, plus one MUFU rsqrt;
+# a quadrupole cell interaction is d (3), d^2 (3), r^2 (1), Q.d (9), d.Q.d (3),
+# r^5 (2), t = 2.5 (d.Q.d) r^2 + m d^2 (3), a += (d t - Q d) r^5 (6) = 30, plus
+# one MUFU rsqrt.  Votes, loads and the compensated TwoSum are overhead.
+OPS_PER_BODY_INTERACTION = 12
+OPS_PER_QUADRUPOLE_CELL = 30
+# DRAM bytes (read + write) of one force launch per body, measured by ncu on
+# the same workload at N = 1,048,576 (390.4 MB read + 75.0 MB written); the
+# tree, and the cells each body opens, grow in proportion to N at fixed
+# theta and distribution, so the per-body figure scales to 4M
+FORCE_DRAM_BYTES_PER_BODY = (390.426624e6 + 75.037696e6) / 1048576
 
 
 # ---------------------------------------------------------------------------
@@ -191,6 +202,26 @@ def workload_ic(nb, n, seed):
     return pos, vel, mass
 
 
+def workload_ic_cpu(n, seed):
+    """The same bytes as workload_ic, from the oracle's restatement of the
+    library's generator (the CPU arm never loads the library)."""
+    from oracle import oracle as O
+    O.build()
+    pos, mass = O.generate_ic(n, seed, O.POS_NORMAL_SIGMA, WORKLOAD["sigma"], mass_mode=O.MASS_LOGNORMAL,
+                              mass_sigma=WORKLOAD["mass_sigma"])
+    return pos, np.zeros_like(pos), mass
+
+
+def step_config(n, world):
+    """The config of the Barnes-Hut step line; both arms print this dict."""
+    return {"workload": WORKLOAD["name"] if n == WORKLOAD["n"] else f"bh_plummer_n{n}_theta0.5", "n_bodies": n,
+            "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"], "dt": WORKLOAD["dt"], "G": WORKLOAD["G"],
+            "integrator": "euler", "precision": WORKLOAD["precision"], "multipole": WORKLOAD["multipole"],
+            "tree": "geometric octree, standard opening criterion, 32-lane warp vote",
+            "l2": "inputs larger than L2 (bodies + tree about 2.3 GB per system)",
+            "parallelism": f"replicas x{world}"}
+
+
 def make_sim(nb, n, precision, device):
     return nb.Simulation(num_of_bodies=n, algo_config=nb.BARNES_HUT, theta=WORKLOAD["theta"],
                          epsilon=WORKLOAD["eps"], gravitational_constant=WORKLOAD["G"], numerical_method=nb.EULER,
@@ -198,40 +229,40 @@ def make_sim(nb, n, precision, device):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle's restatement of the reference kernels, sampled
+# CPU baseline: the oracle's restatement of the reference kernels, whole
+# steps on every host core (oracle/nbpipeline.c)
 # ---------------------------------------------------------------------------
-def cpu_baseline(pos, mass, sample_groups=512, repeats=1):
-    """bbox + build + summarise + sort over all N bodies (sequential C, as the
-    oracle restates them) plus the force walk (OpenMP) for `sample_groups`
-    warp groups of 32 spread over the sorted order, scaled to N."""
+def cpu_steps(pos, vel, mass, steps, warmup):
+    """`warmup` untimed then `steps` timed whole steps of the workload on the
+    CPU: bbox, build, summarise (+ quadrupoles), sort, the force walk of every
+    body (compensated, vote width 32) and the Euler update, each stage on all
+    host threads (OpenMP).  Advances pos/vel in place."""
     from oracle import oracle as O
     O.build()
     n = len(mass)
-    times = []
-    for _ in range(repeats):
-        t0 = time.perf_counter()
-        box = O.bbox_exact(pos)
-        t = O.tree_build(O.SEM_GEOMETRIC, pos, mass, box, 2 * n)
-        O.saturate(t)
-        quad = O.quadrupoles(t)
-        srt, _ = O.sort_bodies(t.children, n, t.root)
-        t1 = time.perf_counter()
-        dq = O.thresholds(O.CRIT_STANDARD, box, WORKLOAD["theta"], WORKLOAD["eps"], t.max_depth)
-        ngroups = n // 32
-        pick = np.linspace(0, ngroups - 1, sample_groups).astype(np.int64)
-        order = (pick[:, None] * 32 + np.arange(32)[None, :]).ravel()
-        order = srt[order]
-        t2 = time.perf_counter()
-        O.bh_force(t, dq, WORKLOAD["eps"], WORKLOAD["G"], vote_width=32, order=order, compensated=True, quad=quad)
-        t3 = time.perf_counter()
-        step = (t1 - t0) + (t3 - t2) * (n / len(order))
-        times.append(step)
-    step = min(times)
-    return {"value": n / step, "unit": "body-updates/s", "cores": int(O.lib().orc_max_threads()), "kind": "port",
-            "sample": (f"N={n}: bbox+build+summarize+sort on all bodies (sequential C), force walk "
-                       f"(OpenMP, {O.lib().orc_max_threads()} threads) on {sample_groups} warp groups "
-                       f"({len(order)} bodies) scaled to N; {step:.2f} s per step"),
-            "seconds_per_step": step}
+    acc = np.zeros_like(pos)
+    pipe = O.Pipeline(n)
+    args = (WORKLOAD["theta"], WORKLOAD["eps"], WORKLOAD["G"], WORKLOAD["dt"])
+    for _ in range(warmup):
+        pipe.step(pos, vel, acc, mass, *args, quadrupole=True, compensated=True)
+    stage = dict.fromkeys(O.PIPE_STAGES, 0.0)
+    inter = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for k, v in pipe.step(pos, vel, acc, mass, *args, quadrupole=True, compensated=True).items():
+            stage[k] += v
+        inter += int(pipe.stats.sum())
+    seconds = time.perf_counter() - t0
+    pipe.close()
+    cores = int(O.lib().orc_max_threads())
+    return {"value": n * steps / seconds, "unit": "body-updates/s", "cores": cores, "kind": "port",
+            "sample": (f"{steps} whole step(s) of all N={n} bodies after {warmup} warm-up step(s): bbox, build, "
+                       f"summarise + quadrupoles, sort, force walk of every body and Euler update, every stage "
+                       f"on {cores} OpenMP threads (oracle/nbpipeline.c; the region counts and the few top "
+                       f"cells of the build are sequential)"),
+            "seconds_per_step": seconds / steps,
+            "stages_s_per_step": {k: round(v / steps, 4) for k, v in stage.items()},
+            "interactions_per_body": inter / steps / n}
 
 
 # ---------------------------------------------------------------------------
@@ -353,10 +384,10 @@ def run_ours(args, dist: Dist):
     sm_mhz = (clk or {}).get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
     sm_count = device_sm_count(dev)
     inter_per_step = inter / args.steps
-    flops_per_step = (FLOPS_PER_INTERACTION * inter + FLOPS_PER_QUADRUPOLE * cell_inter) / args.steps
+    body_inter = inter - cell_inter
+    ops_per_step = (OPS_PER_BODY_INTERACTION * body_inter + OPS_PER_QUADRUPOLE_CELL * cell_inter) / args.steps
     fp32_peak_ops = FP32_LANES_PER_SM * sm_count * sm_mhz * 1e6  # one FP32 op per lane per clock
-    # DRAM bytes of one force launch from the ncu capture at N = 1M
-    # (profiles/k_force_bh_n1m_theta0.5_quadrupole.md), scaled by bodies
+    achieved_ops = ops_per_step / (force_ms / 1e3)
     traffic = FORCE_DRAM_BYTES_PER_BODY * n
     out = {
         "metric": "BH body-updates/s N=4M theta=0.5 (RMS force err <= 1e-3)",
@@ -371,12 +402,7 @@ def run_ours(args, dist: Dist):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded normal sigma=(1,1,0.2) positions, lognormal masses)",
-        "config": {"workload": WORKLOAD["name"] if n == WORKLOAD["n"] else f"bh_plummer_n{n}_theta0.5", "n_bodies": n, "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"],
-                   "dt": dt, "G": WORKLOAD["G"], "integrator": "euler", "precision": WORKLOAD["precision"],
-                   "multipole": WORKLOAD["multipole"],
-                   "tree": "geometric octree, standard opening criterion, 32-lane warp vote",
-                   "l2": "inputs larger than L2 (bodies + tree about 2.3 GB per system)",
-                   "parallelism": f"replicas x{dist.world}"},
+        "config": step_config(n, dist.world),
         "e2e": {"value": e2e_value, "unit": "body-updates/s", "h2d_bytes_per_step": 28 * n,
                 "d2h_bytes_per_step": 24 * n + 64},
         "gpu_launches": int(launches),
@@ -384,48 +410,47 @@ def run_ours(args, dist: Dist):
         "accuracy": {"rms_rel_err": err_rms, "max_rel_err": err_max, "samples": PROBE_SAMPLES,
                      "oracle": "FP64 direct sum on the GPU", "gate_rms_le_1e-3": bool(err_rms <= 1e-3)},
         "fp32_accumulation_value": fp32_value,
-        "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
-                     "algorithmic_bytes": alg_bytes, "peak_kind": f"{peak_kind} hbm copy",
-                     "note": "the force walk is latency / FP32-bound; see compute"},
-        "compute": {"bound": "fp32", "kernel": "k_force", "interactions_per_step": inter_per_step,
+        "roofline": {"bound": "fp32", "kernel": "k_force", "achieved": achieved_ops / 1e12,
+                     "peak": fp32_peak_ops / 1e12, "unit": "T FP32-pipe ops/s",
+                     "frac": achieved_ops / fp32_peak_ops, "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                     "traffic_over_algorithmic": traffic / alg_bytes,
+                     "ops_per_step": ops_per_step,
+                     "ops_model": (f"{OPS_PER_BODY_INTERACTION} FP32-pipe ops per body interaction, "
+                                   f"{OPS_PER_QUADRUPOLE_CELL} per quadrupole cell interaction"),
+                     "peak_kind": (f"derived: {FP32_LANES_PER_SM} FP32 lanes x {sm_count} SMs x "
+                                   f"{sm_mhz:.0f} MHz (no FP32 figure is measured; the walk is bound by "
+                                   f"instruction issue on the FP32 pipe, not by memory)"),
+                     "hbm": {"achieved_gbs": achieved, "peak_gbs": peaks["hbm_gbs"],
+                             "frac": achieved / peaks["hbm_gbs"], "peak_kind": f"{peak_kind} hbm copy"}},
+        "compute": {"kernel": "k_force", "interactions_per_step": inter_per_step,
+                    "body_interactions_per_step": body_inter / args.steps,
                     "cell_interactions_per_step": cell_inter / args.steps,
                     "interactions_per_s": inter_per_step / (force_ms / 1e3),
-                    "achieved_gops": flops_per_step / (force_ms / 1e3) / 1e9,
-                    "peak_gops": fp32_peak_ops / 1e9,
-                    "frac": flops_per_step / (force_ms / 1e3) / fp32_peak_ops,
-                    "cells_opened_per_step": opened / args.steps,
-                    "ops_model": "12 FP32 ops per interaction + 19 per cell quadrupole term",
-                    "peak_kind": "derived: 128 FP32 lanes x SMs x maximum SM clock"},
+                    "cells_opened_per_step": opened / args.steps},
         "tree": {"cells_used": cells_used, "max_depth": int(info[3])},
         "stages_roofline": stage_roofline(stage, n, cells_used, peaks["hbm_gbs"]),
         "clocks": clk,
     }
     if not args.skip_cpu:
-        out["cpu_baseline"] = cpu_baseline(pos, mass)
+        cpos, cvel, cmass = workload_ic_cpu(n, seed=0)
+        out["cpu_baseline"] = cpu_steps(cpos, cvel, cmass, steps=1, warmup=1)
     return out
 
 
 def run_reference(args, dist: Dist):
-    """The reference's CPU path as restated by the oracle, all host threads."""
+    """The reference's step on the CPU: the oracle's restatement of its
+    kernels (oracle/, OpenMP on every host thread), whole steps of all N
+    bodies, the same workload and config as our arm.  The GPU library is not
+    loaded.  Rank 0 alone runs it."""
     if dist.rank != 0:
         return None
-    import nbodysimulation_gb300 as nb
-    from nbodysimulation_gb300 import build as nbbuild
-    nbbuild.build()
     n = args.n
-    pos, _, mass = workload_ic(nb, n, seed=0)
-    for _ in range(args.warmup):
-        cpu_baseline(pos, mass, sample_groups=64)
+    pos, vel, mass = workload_ic_cpu(n, seed=0)
     t0 = time.perf_counter()
-    per = []
-    for _ in range(args.steps):
-        per.append(cpu_baseline(pos, mass, sample_groups=128))
+    cb = cpu_steps(pos, vel, mass, steps=args.steps, warmup=args.warmup)
     wall = time.perf_counter() - t0
-    step_s = sum(p["seconds_per_step"] for p in per) / len(per)
-    value = n / step_s
-    cb = dict(per[-1])
-    cb["value"] = value
+    value = cb["value"]
+    cb["wall_s_with_warmup"] = wall
     return {
         "impl": "reference",
         "metric": "BH body-updates/s N=4M theta=0.5 (RMS force err <= 1e-3)",
@@ -434,15 +459,13 @@ def run_reference(args, dist: Dist):
         "n_gpus": dist.world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": step_s * 1e3,
+        "ms_per_step": cb["seconds_per_step"] * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded normal sigma=(1,1,0.2) positions, lognormal masses)",
-        "config": {"workload": WORKLOAD["name"] if n == WORKLOAD["n"] else f"bh_plummer_n{n}_theta0.5", "n_bodies": n, "theta": WORKLOAD["theta"], "eps": WORKLOAD["eps"],
-                   "dt": WORKLOAD["dt"], "precision": WORKLOAD["precision"], "multipole": WORKLOAD["multipole"],
-                   "wall_s": wall},
+        "config": step_config(n, dist.world),
         "cpu_baseline": cb,
         "e2e": {"value": value, "unit": "body-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

@@ -27,14 +27,7 @@
 #include <omp.h>
 #endif
 
-#define ORC_EMPTY (-1)
-#define ORC_MAX_DEPTH 64
-
-enum { ORC_OK = 0, ORC_ERR_CELL_OVERFLOW = 4, ORC_ERR_DEPTH = 5, ORC_ERR_ARG = 1 };
-enum { ORC_SEM_REFERENCE = 0, ORC_SEM_GEOMETRIC = 1 };
-enum { ORC_CRIT_REFERENCE = 0, ORC_CRIT_STANDARD = 1 };
-enum { ORC_ARITH_REFERENCE = 0, ORC_ARITH_FMA = 1 };
-enum { ORC_LEAPFROG = 1, ORC_EULER = 2, ORC_KDK = 3 };
+#include "nboracle.h"
 
 int orc_version(void) { return 1; }
 
@@ -57,15 +50,6 @@ void orc_set_threads(int n) {
 /* ------------------------------------------------------------------ */
 /* Bounding box                                                        */
 /* ------------------------------------------------------------------ */
-
-/* Order-preserving key of a float: an unsigned compare on keys is the float
- * order with -0 < +0.  The GPU reduction uses the same total order, which
- * makes the exact bounding box bit-reproducible. */
-static inline uint32_t orc_fkey(float f) {
-    uint32_t b;
-    memcpy(&b, &f, 4);
-    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
 
 /* True component-wise min/max over all bodies: what boundary_reduce
  * (kernels/boundary_reduce.cl:6-160) is meant to compute. */
@@ -122,19 +106,9 @@ static inline void orc_adjust_ref(const float p[3], float bmin[3], float bmax[3]
     if (dz > 0) bmin[2] = c[2]; else bmax[2] = c[2];
 }
 
-/* Geometric semantics: a cubic root around the box centre with half-width
- * 0.5*max extent (Burtscher), octant 4*(y<cy)+2*(x<cx)+(z<cz) (the
- * reference's numbering), child centre = centre -/+ r/2 per axis. */
-typedef struct { float c[3]; float r; } orc_cube;
-
-static inline int orc_octant_geo(const float p[3], const orc_cube *q) {
-    return (p[1] < q->c[1] ? 4 : 0) + (p[0] < q->c[0] ? 2 : 0) + (p[2] < q->c[2] ? 1 : 0);
-}
-static inline void orc_descend_geo(const float p[3], orc_cube *q) {
-    q->r *= 0.5f;
-    for (int k = 0; k < 3; ++k) q->c[k] += (p[k] < q->c[k]) ? -q->r : q->r;
-}
-
+/* Geometric semantics (orc_cube, orc_octant_geo, orc_descend_geo in
+ * nboracle.h): a cubic root around the box centre with half-width 0.5*max
+ * extent (Burtscher), the reference's octant numbering. */
 void orc_root_cube(const float box6[6], float out4[4]) {
     float ex = box6[3] - box6[0], ey = box6[4] - box6[1], ez = box6[5] - box6[2];
     float m = ex > ey ? ex : ey;
@@ -313,8 +287,14 @@ int orc_tree_paths(const int *children, int n, int root, int maxlen, signed char
  * equals the slot number, :60); 0 compacts correctly. */
 int orc_saturate(int compaction_bug, int n, int nodes, int bottom, float *node_pos, float *node_mass,
                  int *children, int *body_count) {
-    const int root = n + nodes;
-    for (int c = bottom; c <= root; ++c) {
+    return orc_saturate_range(compaction_bug, n, bottom, n + nodes, node_pos, node_mass, children, body_count);
+}
+
+/* The same over the cells [lo, hi] only, ascending: every child of a cell in
+ * the range is a body or a cell below it that is already summarised. */
+int orc_saturate_range(int compaction_bug, int n, int lo, int hi, float *node_pos, float *node_mass,
+                       int *children, int *body_count) {
+    for (int c = lo; c <= hi; ++c) {
         int *row = children + (long)c * 8;
         float M = 0.0f, cx = 0.0f, cy = 0.0f, cz = 0.0f;
         int count = 0, used = 0;
@@ -352,9 +332,15 @@ int orc_saturate(int compaction_bug, int n, int nodes, int bottom, float *node_p
  * Q = 0.  quad[6*node] = {xx, yy, zz, xy, xz, yz}. */
 void orc_quadrupoles(int n, int nodes, int bottom, const float *node_pos, const float *node_mass,
                      const int *children, float *quad) {
-    const int root = n + nodes;
     for (long i = 0; i < (long)(n + nodes + 1) * 6; ++i) quad[i] = 0.0f;
-    for (int c = bottom; c <= root; ++c) {
+    orc_quadrupoles_range(n, bottom, n + nodes, node_pos, node_mass, children, quad);
+}
+
+/* The same for the cells [lo, hi] only, ascending (children first); the
+ * entries of bodies are never read. */
+void orc_quadrupoles_range(int n, int lo, int hi, const float *node_pos, const float *node_mass,
+                           const int *children, float *quad) {
+    for (int c = lo; c <= hi; ++c) {
         const int *row = children + (long)c * 8;
         const float X = node_pos[c * 3 + 0], Y = node_pos[c * 3 + 1], Z = node_pos[c * 3 + 2];
         float q[6] = {0, 0, 0, 0, 0, 0};
@@ -495,51 +481,73 @@ int orc_bh_force(const float *node_pos, const float *node_mass, const int *child
                     const float cxp = node_pos[child * 3 + 0], cyp = node_pos[child * 3 + 1],
                                 czp = node_pos[child * 3 + 2], cm = node_mass[child];
                     float d2v[64], dxv[64], dyv[64], dzv[64];
+                    const float thr = dq[depth];
                     int all = 1;
-                    for (int l = 0; l < lanes; ++l) {
-                        float dx = cxp - px[l], dy = cyp - py[l], dz = czp - pz[l];
-                        float d2;
-                        if (arith == ORC_ARITH_REFERENCE)
-                            d2 = eps2 + dx * dx + dy * dy + dz * dz;
-                        else
-                            d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-                        dxv[l] = dx; dyv[l] = dy; dzv[l] = dz; d2v[l] = d2;
-                        if (!(d2 >= dq[depth])) all = 0;
+                    /* lane loops are written without early exits so that the
+                     * compiler can vectorise them; every lane's arithmetic is
+                     * the scalar sequence above, so results do not change */
+                    if (arith == ORC_ARITH_REFERENCE) {
+                        for (int l = 0; l < lanes; ++l) {
+                            const float dx = cxp - px[l], dy = cyp - py[l], dz = czp - pz[l];
+                            const float d2 = eps2 + dx * dx + dy * dy + dz * dz;
+                            dxv[l] = dx; dyv[l] = dy; dzv[l] = dz; d2v[l] = d2;
+                            all &= d2 >= thr;
+                        }
+                    } else {
+                        for (int l = 0; l < lanes; ++l) {
+                            const float dx = cxp - px[l], dy = cyp - py[l], dz = czp - pz[l];
+                            const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+                            dxv[l] = dx; dyv[l] = dy; dzv[l] = dz; d2v[l] = d2;
+                            all &= d2 >= thr;
+                        }
                     }
                     if (child < n || all) {
+                        /* F per lane; a body's own entry (skip_self) gets F = 0,
+                         * which adds exactly nothing below */
+                        float Fv[64], rv[64];
+                        int self = 0;
                         for (int l = 0; l < lanes; ++l) {
-                            if (skip_self && child == body[l]) continue;
-                            float r = 1.0f / sqrtf(d2v[l]);
-                            float F;
-                            if (arith == ORC_ARITH_REFERENCE) F = cm * r * r * r;
-                            else F = (cm * r) * (r * r);
-                            float tx, ty, tz;
+                            const float r = 1.0f / sqrtf(d2v[l]);
+                            float F = arith == ORC_ARITH_REFERENCE ? cm * r * r * r : (cm * r) * (r * r);
+                            const int me = skip_self && child == body[l];
+                            self += me;
+                            rv[l] = r;
+                            Fv[l] = me ? 0.0f : F;
+                        }
+                        if (!compensated) {
                             if (arith == ORC_ARITH_REFERENCE) {
-                                tx = dxv[l] * F; ty = dyv[l] * F; tz = dzv[l] * F;
-                                if (!compensated) { ax[l] = ax[l] + tx; ay[l] = ay[l] + ty; az[l] = az[l] + tz; }
-                            } else {
-                                if (!compensated) {
-                                    ax[l] = fmaf(dxv[l], F, ax[l]);
-                                    ay[l] = fmaf(dyv[l], F, ay[l]);
-                                    az[l] = fmaf(dzv[l], F, az[l]);
+                                for (int l = 0; l < lanes; ++l) {
+                                    ax[l] = ax[l] + dxv[l] * Fv[l];
+                                    ay[l] = ay[l] + dyv[l] * Fv[l];
+                                    az[l] = az[l] + dzv[l] * Fv[l];
                                 }
-                                tx = dxv[l] * F; ty = dyv[l] * F; tz = dzv[l] * F;
+                            } else {
+                                for (int l = 0; l < lanes; ++l) {
+                                    ax[l] = fmaf(dxv[l], Fv[l], ax[l]);
+                                    ay[l] = fmaf(dyv[l], Fv[l], ay[l]);
+                                    az[l] = fmaf(dzv[l], Fv[l], az[l]);
+                                }
                             }
-                            if (compensated) {
-                                /* TwoSum (Knuth): s = a+b exactly split into s + e */
+                        } else {
+                            /* TwoSum (Knuth): s = a+b exactly split into s + e */
+                            for (int l = 0; l < lanes; ++l) {
+                                const float tx = dxv[l] * Fv[l], ty = dyv[l] * Fv[l], tz = dzv[l] * Fv[l];
                                 float s, bp, e;
                                 s = ax[l] + tx; bp = s - ax[l]; e = (ax[l] - (s - bp)) + (tx - bp); ax[l] = s; lx[l] += e;
                                 s = ay[l] + ty; bp = s - ay[l]; e = (ay[l] - (s - bp)) + (ty - bp); ay[l] = s; ly[l] += e;
                                 s = az[l] + tz; bp = s - az[l]; e = (az[l] - (s - bp)) + (tz - bp); az[l] = s; lz[l] += e;
                             }
-                            if (quad && child >= n) {
-                                /* softened quadrupole of the cell about its centre of mass:
-                                 * a += 2.5 (d.Q.d) d / r^7 - Q d / r^5, d = x_cell - x_body */
-                                const float *Q = quad + (long)child * 6; /* xx yy zz xy xz yz */
-                                const float dx = dxv[l], dy = dyv[l], dz = dzv[l];
-                                const float qx = fmaf(Q[4], dz, fmaf(Q[3], dy, Q[0] * dx));
-                                const float qy = fmaf(Q[5], dz, fmaf(Q[1], dy, Q[3] * dx));
-                                const float qz = fmaf(Q[2], dz, fmaf(Q[5], dy, Q[4] * dx));
+                        }
+                        if (quad && child >= n) {
+                            /* softened quadrupole of the cell about its centre of mass:
+                             * a += 2.5 (d.Q.d) d / r^7 - Q d / r^5, d = x_cell - x_body */
+                            const float *Q = quad + (long)child * 6; /* xx yy zz xy xz yz */
+                            const float Qxx = Q[0], Qyy = Q[1], Qzz = Q[2], Qxy = Q[3], Qxz = Q[4], Qyz = Q[5];
+                            for (int l = 0; l < lanes; ++l) {
+                                const float dx = dxv[l], dy = dyv[l], dz = dzv[l], r = rv[l];
+                                const float qx = fmaf(Qxz, dz, fmaf(Qxy, dy, Qxx * dx));
+                                const float qy = fmaf(Qyz, dz, fmaf(Qyy, dy, Qxy * dx));
+                                const float qz = fmaf(Qzz, dz, fmaf(Qyz, dy, Qxz * dx));
                                 const float sq = fmaf(dz, qz, fmaf(dy, qy, dx * qx));
                                 const float r2i = r * r;
                                 const float r5 = (r * r2i) * r2i;
@@ -555,10 +563,10 @@ int orc_bh_force(const float *node_pos, const float *node_mass, const int *child
                                     s = az[l] + uz; bp = s - az[l]; e = (az[l] - (s - bp)) + (uz - bp); az[l] = s; lz[l] += e;
                                 }
                             }
-                            if (stats) {
-                                if (child < n) ++nb_body;
-                                else ++nb_cell;
-                            }
+                        }
+                        if (stats) {
+                            if (child < n) nb_body += lanes - self;
+                            else nb_cell += lanes - self;
                         }
                     } else {
                         ++depth;
@@ -731,6 +739,7 @@ int orc_direct_quirk_local(const float *pos3, const float *mass, int n, int wg, 
  * Any other method changes nothing (the as-wired BH path binds NumberOfBodies as the method). */
 void orc_integrate(int method, int primed, int n, float dt, const float *acc_new3, float *accs3, float *vel3,
                    float *pos3, int pos_stride) {
+#pragma omp parallel for schedule(static) if (n >= 65536)
     for (int i = 0; i < n; ++i) {
         float *x = pos3 + (long)i * pos_stride, *v = vel3 + i * 3, *ap = accs3 + i * 3;
         const float *a = acc_new3 + i * 3;

@@ -58,6 +58,12 @@ def lib():
             "orc_copy_vertices": ([P, i, P], None),
             "orc_max_threads": ([], i),
             "orc_set_threads": ([i], None),
+            "orc_generate_ic": ([i, ctypes.c_uint64, i, P, f, i, f, P, P], i),
+            "orc_pipe_create": ([i, i], P),
+            "orc_pipe_destroy": ([P], None),
+            "orc_pipe_step": ([P, P, P, P, P, f, f, f, f, i, i, P, P], i),
+            "orc_pipe_export": ([P, P, P, P], i),
+            "orc_pipe_levels_of": ([P], i),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -273,3 +279,71 @@ def bh_step_forces(pos3, mass, theta, eps, G, sem=SEM_GEOMETRIC, criterion=CRIT_
     if rc:
         raise RuntimeError(f"oracle force failed: {rc}")
     return acc, t, srt
+
+
+# ---------------------------------------------------------------------------
+# seeded initial conditions and the parallel whole step (nbpipeline.c)
+# ---------------------------------------------------------------------------
+POS_UNIFORM, POS_NORMAL_SIGMA = 1, 3
+MASS_EQUAL, MASS_LOGNORMAL = 1, 2
+PIPE_STAGES = ("bbox", "build", "summarize", "sort", "force", "integrate")
+
+
+def generate_ic(n, seed, pos_mode=POS_NORMAL_SIGMA, sigma=(1.0, 1.0, 1.0), radius=1.0, mass_mode=MASS_EQUAL,
+                mass_sigma=0.5):
+    """Positions and masses of the library's seeded generator (the same
+    bytes as nb_generate_ic for these modes), without the library."""
+    pos = np.zeros((n, 3), np.float32)
+    mass = np.zeros(n, np.float32)
+    sg = np.asarray(sigma, np.float32)
+    rc = lib().orc_generate_ic(n, seed, pos_mode, _p(sg), radius, mass_mode, mass_sigma, _p(pos), _p(mass))
+    if rc:
+        raise ValueError(f"orc_generate_ic: unsupported mode ({rc})")
+    return pos, mass
+
+
+class Pipeline:
+    """One whole Barnes-Hut step (bbox, build, summarise, sort, force, Euler)
+    on every host core, results equal to the sequential restatement.
+    Geometric tree, standard criterion, vote width 32."""
+
+    def __init__(self, n, nodes=None):
+        self.n = n
+        self.nodes = 2 * n if nodes is None else nodes
+        self.h = lib().orc_pipe_create(n, self.nodes)
+        if not self.h:
+            raise MemoryError("orc_pipe_create failed")
+        self.stage_s = np.zeros(6, np.float64)
+        self.stats = np.zeros(2, np.int64)
+
+    @property
+    def levels(self):
+        return lib().orc_pipe_levels_of(self.h)
+
+    def step(self, pos, vel, acc, mass, theta, eps, G, dt, quadrupole=True, compensated=True):
+        """Advances pos/vel (float32 [n,3], in place); acc receives the new
+        accelerations.  Returns the stage seconds as a dict."""
+        for a in (pos, vel, acc):
+            assert a.dtype == np.float32 and a.flags.c_contiguous and a.size == 3 * self.n
+        rc = lib().orc_pipe_step(self.h, _p(pos), _p(vel), _p(acc), _p(f32(mass)), theta, eps, G, dt,
+                                 1 if quadrupole else 0, 1 if compensated else 0, _p(self.stage_s), _p(self.stats))
+        if rc:
+            raise RuntimeError(f"orc_pipe_step failed: {rc}")
+        return dict(zip(PIPE_STAGES, self.stage_s.tolist()))
+
+    def export(self):
+        """(children rows, sorted order, bottom, max_depth) of the last step."""
+        total = self.n + self.nodes + 1
+        ch = np.empty(total * 8, np.int32)
+        srt = np.empty(self.n, np.int32)
+        info = np.zeros(2, np.int32)
+        lib().orc_pipe_export(self.h, _p(ch), _p(srt), _p(info))
+        return ch, srt, int(info[0]), int(info[1])
+
+    def close(self):
+        if self.h:
+            lib().orc_pipe_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -14,7 +14,23 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("NBGB_REFERENCE_DIR", "/root/reference")
+def _recipe_reference_dir():
+    """The reference sources: NBGB_REFERENCE_DIR, else the default that the
+    build recipe (ref/Makefile, `REF ?= ...`) reads them from."""
+    env = os.environ.get("NBGB_REFERENCE_DIR")
+    if env:
+        return env
+    try:
+        with open(os.path.join(HERE, "ref", "Makefile")) as f:
+            for line in f:
+                if line.startswith("REF ?="):
+                    return line.split("?=", 1)[1].strip()
+    except OSError:
+        pass
+    return ""
+
+
+REF_SRC = _recipe_reference_dir()
 WGS = (16, 64, 256)
 
 
