@@ -276,14 +276,18 @@ void nb_host_free(void *p);
  * Computes a_i = G * sum_{j != i} m_j r_ij (|r_ij|^2 + eps^2)^-3/2 for the n
  * bodies of d_body4 (device float4 {x,y,z,m}, 16-byte aligned) into d_acc4
  * (device float4 {ax,ay,az,0}, 16-byte aligned), on `stream` (a
- * cudaStream_t; NULL for the default stream) of the current device, and
- * waits for it.  Same arithmetic as the NB_BRUTE_FORCE_LOCAL Plummer sum.
+ * cudaStream_t; NULL for the default stream) of the current device.  The
+ * call is synchronous: it returns after its work on `stream` has finished
+ * (it synchronises that stream to read the status of its bounded waits).
+ * Same arithmetic as the NB_BRUTE_FORCE_LOCAL Plummer sum.
  *
  * Limit: n <= NB_NOALLOC_MAX_BODIES; larger n returns NB_ERR_INVALID_ARGUMENT.
  * Its scratch is a fixed array inside the library (1 MiB), held by every GPU
  * that loads the library until the process exits.  The first call on a
  * device looks up that array's device address; make that first call before
- * any stream capture.  All calls share the array, so calls that overlap on
+ * any stream capture.  The address is kept for the life of the process, so
+ * after a cudaDeviceReset of a device this entry point must not be called on
+ * that device again.  All calls share the array, so calls that overlap on
  * the GPU race: serialise them. */
 #define NB_NOALLOC_MAX_BODIES 65536
 nb_status nb_direct_accel_noalloc(const float *d_body4, int32_t n, float eps, float G, float *d_acc4,

@@ -607,10 +607,15 @@ __global__ void k_noalloc_finish(const float4 *__restrict__ part, int n, float G
 
 #include "../../include/nbgb.h"
 
+static_assert(nbgb::kNoAllocMaxBodies == NB_NOALLOC_MAX_BODIES, "the scratch must hold the documented limit");
+
 namespace {
 // Device addresses of the two arrays, looked up once per device with that
 // device current.  In host code the array names are host-side stand-ins, not
 // device addresses, so only these looked-up pointers are passed to kernels.
+// The addresses are kept for the life of the process: a cudaDeviceReset (or
+// a reset of the device's primary context) unloads the module, after which
+// this entry point must not be called on that device again.
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void *g_noalloc_part_ptr[kMaxDevices] = {};
