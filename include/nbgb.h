@@ -245,7 +245,13 @@ nb_status nb_get_state_device(nb_sim *sim, float *d_pos3, float *d_vel3);
 nb_status nb_force_error_probe(nb_sim *sim, const int32_t *sample, int32_t ns, double *max_rel, double *rms_rel,
                                double *rel_err);
 /* out[0..8]: kinetic energy, momentum xyz, angular momentum xyz, total mass,
- * potential energy (FP64 pair sum; computed only when with_potential != 0). */
+ * potential energy (FP64 pair sum; computed only when with_potential != 0).
+ * Every sum is over the stored state, the one nb_get_state returns.  Under
+ * NB_KDK_LEAPFROG the stored velocities are the half-step velocities
+ * v(t - dt/2) of the drift that produced the positions x(t), so the kinetic
+ * energy, momentum and angular momentum are those of v(t - dt/2) (with x(t)
+ * for the angular momentum); under NB_EULER and NB_LEAPFROG velocity and
+ * position belong to the same step. */
 nb_status nb_diagnostics(nb_sim *sim, int32_t with_potential, double out[9]);
 
 /* ---- failure-path test hook ----
