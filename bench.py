@@ -23,6 +23,7 @@ The same line carries more measurements, each with its own timed region
            their FP64-probe accuracy;
   direct   the TMA-tiled direct sum on N = 262,144 (interactions/s against
            the FP32-pipe roofline) and the naive kernel on N = 4096;
+  collision  the collision update on the 262,144-body unit ball (pairs/s);
   batched  512 systems, N log-uniform in [1024, 262144], one CUDA graph per
            step, against a loop of plain solves (one handle per system);
   serving  a seeded Poisson job stream (200 jobs/s; N log-uniform in
@@ -600,6 +601,52 @@ def run_direct(args, dist: Dist):
 
 
 # ---------------------------------------------------------------------------
+# collision update (update_collision_local) on the 262,144-body unit ball
+# ---------------------------------------------------------------------------
+COLLIDE = dict(n=262144, steps=10)
+
+
+def run_collision(args, dist: Dist):
+    """CUDA-event time of the collision stage inside Barnes-Hut steps of the
+    plain configuration's bodies (unit ball, circular velocities, masses
+    1/N, theta 0.5, eps 0.01) with collision on.  Every ordered pair is
+    tested, so pairs/s = N^2 / stage time.  Roofline: the exact test of a
+    pair needs at least its x separation, one FP32-pipe operation, so pairs/s
+    over 128 FP32 lanes x SMs x clock is an upper bound of the fraction."""
+    import nbodysimulation_gb300 as nb
+    dev = dist.local_rank
+    n = COLLIDE["n"]
+    cfg = nb.default_config(num_of_bodies=n, algo_config=nb.BARNES_HUT, theta=BALL["theta"], epsilon=BALL["eps"],
+                            gravitational_constant=BALL["G"], numerical_method=nb.EULER, device=dev,
+                            pos_config=nb.BALL_POS, starting_volume_radius=1.0, vel_config=nb.CIRCULAR_Z_VEL,
+                            mass_config=nb.MASS_EQUAL, seed=0, collision=1)
+    pos, vel, mass = nb.generate_ic(cfg)
+    with nb.Simulation(cfg) as s:
+        s.set_state(pos, mass, vel)
+        s.set_profiling(True)
+        s.step(BALL["dt"], args.warmup)
+        ms = s.time_steps(BALL["dt"], COLLIDE["steps"])
+        stage = s.timings()
+    if dist.rank != 0:
+        return None
+    peaks, _ = measured_peaks()
+    sm_count = device_sm_count(dev)
+    mhz = peaks.get("sm_max_mhz", 2070.0)
+    coll_ms = stage["collision"]
+    pairs = float(n) * n
+    pps = pairs / (coll_ms / 1e3)
+    peak = FP32_LANES_PER_SM * sm_count * mhz * 1e6
+    return {"workload": "collision_ball_n262144 (Barnes-Hut steps with collision on; unit ball, masses 1/N)",
+            "kernel": "k_collision (block form, targets in sort order)", "n_bodies": n,
+            "steps": COLLIDE["steps"], "ms_per_step": ms / COLLIDE["steps"], "collision_ms": coll_ms,
+            "stages_ms": {k: round(v, 4) for k, v in stage.items() if v > 0},
+            "pairs_per_s": pps,
+            "roofline": {"bound": "fp32", "achieved": pps / 1e12, "peak": peak / 1e12,
+                         "unit": "T pairs/s at one FP32-pipe op per pair", "frac": pps / peak,
+                         "peak_kind": "derived: 128 FP32 lanes x SMs x maximum SM clock"}}
+
+
+# ---------------------------------------------------------------------------
 # batched systems vs a loop of plain solves
 # ---------------------------------------------------------------------------
 BATCH = dict(name="batch512_loguniform_1k_256k", systems=512, n_min=1024, n_max=262144, direct_below=8192,
@@ -924,7 +971,7 @@ def main():
                 # timed region (see their modes): direct sum, batched systems
                 # against plain solves, the job server against plain solves
                 extra = {"bh_configs": run_bh_configs(args, dist), "direct": run_direct(args, dist),
-                         "batched": run_batch(args, dist)}
+                         "collision": run_collision(args, dist), "batched": run_batch(args, dist)}
                 if args.serve_seconds is None:
                     args.serve_seconds = SERVE["seconds_in_step"]
                 extra["serving"] = run_serve(args, dist)

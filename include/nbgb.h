@@ -323,9 +323,12 @@ nb_status nb_save_snapshot(nb_sim *sim, const char *path, int64_t step, double t
  * algo_config NB_BARNES_HUT take the tree path, the others the tiled direct
  * sum.  All systems must share numerical_method, precision, multipole and
  * device; epsilon (direct_epsilon for direct systems) must be > 0; the
- * reference quirk force law and collisions are not batched.  Each system's
- * step is the same computation as nb_step on a standalone handle: the tree
- * path is bit-identical, the direct sum differs only in summation order. */
+ * reference quirk force law is not batched.  Systems with collision != 0 run
+ * the collision update after their integration, as a standalone handle does
+ * (one more launch per step over all of them).  Each system's step is the
+ * same computation as nb_step on a standalone handle: the tree path and the
+ * collision update are bit-identical, the direct sum differs only in
+ * summation order. */
 typedef struct nb_batch nb_batch;
 nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out);
 nb_status nb_batch_destroy(nb_batch *b);

@@ -484,7 +484,7 @@ static nb_status enqueue_step(nb_sim *s, float dt, int timed) {
         s->stage_ran[kStDirect] = true;
     }
     if (c.collision) {
-        NB_CUDA(s, launch_collision(d, s->sm_count, st));
+        NB_CUDA(s, launch_collision(d, s->tree ? 1 : 0, s->sm_count, st));
         s->launches += 1;
         s->stage_ran[kStCollision] = true;
     }

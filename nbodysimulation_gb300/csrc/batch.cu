@@ -34,7 +34,7 @@ struct nb_batch {
     Ctrl *h_ctrl = nullptr;     // pinned mirror
     std::vector<SysDesc> h_sys;
     SysDesc *d_sys = nullptr;
-    int *d_pref = nullptr;      // 5 prefix tables of nsys + 1 (the last written on the device)
+    int *d_pref = nullptr;      // prefix tables of nsys + 1 (batch_prefix_device_ints; the last written on the device)
     int *d_work = nullptr;
     float *d_stage = nullptr;   // 4 * max N floats of transfer staging
     BatchTables t{};
@@ -74,11 +74,11 @@ static void drop_graph(nb_batch *b) {
     b->graph = nullptr;
 }
 
-// Work offsets of every system in the four batch-wide index spaces.
+// Work offsets of every system in the batch-wide index spaces.
 static nb_status rebuild_tables(nb_batch *b) {
     const int ns = b->nsys;
-    std::vector<int> pref(4 * (size_t)(ns + 1), 0);
-    int totals[4];
+    std::vector<int> pref(batch_prefix_ints(ns), 0);
+    int totals[kBatchSpaces];
     batch_prefixes(b->h_sys.data(), ns, batch_direct_block_bodies(b->variant), pref.data(), totals);
     B_CUDA(b, cudaMemcpyAsync(b->d_sys, b->h_sys.data(), sizeof(SysDesc) * ns, cudaMemcpyHostToDevice, b->st));
     B_CUDA(b, cudaMemcpyAsync(b->d_pref, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, b->st));
@@ -149,7 +149,6 @@ nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out) {
             return NB_ERR_UNSUPPORTED;
         if (c.algo_config < NB_BARNES_HUT || c.algo_config > NB_BRUTE_FORCE_LOCAL) return NB_ERR_INVALID_ARGUMENT;
         if (c.algo_config != NB_BARNES_HUT && c.force_law != NB_FORCE_PLUMMER) return NB_ERR_UNSUPPORTED;
-        if (c.collision) return NB_ERR_UNSUPPORTED;
         const float eps = c.algo_config == NB_BARNES_HUT ? c.epsilon
                                                          : (c.direct_epsilon >= 0.0f ? c.direct_epsilon : c.epsilon);
         if (!(eps > 0.0f)) return NB_ERR_UNSUPPORTED;
@@ -200,7 +199,7 @@ nb_status nb_batch_create(const nb_config *cfgs, int32_t nsys, nb_batch **out) {
     if (cudaMalloc(&b->d_ctrl, sizeof(Ctrl) * nsys) != cudaSuccess ||
         cudaMallocHost(&b->h_ctrl, sizeof(Ctrl) * nsys) != cudaSuccess ||
         cudaMalloc(&b->d_sys, sizeof(SysDesc) * nsys) != cudaSuccess ||
-        cudaMalloc(&b->d_pref, sizeof(int) * 5 * (size_t)(nsys + 1)) != cudaSuccess ||
+        cudaMalloc(&b->d_pref, sizeof(int) * batch_prefix_device_ints(nsys)) != cudaSuccess ||
         cudaMalloc(&b->d_work, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&b->d_stage, sizeof(float) * 4 * (size_t)maxn) != cudaSuccess)
         return fail_all(NB_ERR_OUT_OF_MEMORY);

@@ -9,6 +9,7 @@
 // build, used-cell scan, summarize, sort, force, direct, flip -- captured
 // once into a CUDA graph by the host.
 #include "bh_device.cuh"
+#include "collide_device.cuh"
 #include "force_device.cuh"
 #include "tma.cuh"
 
@@ -433,6 +434,24 @@ __global__ void k_batch_flip(BatchTables t) {
 }
 
 // ---------------------------------------------------------------------------
+// collision update of every system that asks for it (update_collision_local,
+// kernels/collision_update.cl:17-83): one block per kCollideBlockBodies
+// targets of one system (a tree system's in the order of its sort), the
+// block form of the standalone kernel
+// (collide_device.cuh), after the force and direct stages have integrated
+// and before the flip (src/MyApp.cpp:593-596,606-610,622-625).  Systems with
+// no steps left or a failed step are skipped.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kCollideThreads) k_batch_collision(BatchTables t) {
+    const int k = find_system(t.cblock_prefix, t.nsys, blockIdx.x);
+    const SysDesc &d = t.sys[k];
+    if (!system_live(d.v.ctrl) || read_status(d.v.ctrl)) return;  // block-uniform, before any barrier
+    const DevSim s = system_view(d);
+    collide_block(s.body_next, s.vel, d.kind == kSysBH ? s.sorted : nullptr, s.n,
+                  (blockIdx.x - d.cblock_begin) * kCollideThreads, s.ctrl);
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 static int resident(const void *fn, int threads, int sm_count) {
@@ -540,6 +559,10 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
     }
     if (t.dblocks > 0 && !branch) {
         if ((e = launch_direct_variant(t, direct_variant, st)) != cudaSuccess) return e;
+        nl += 1;
+    }
+    if (t.cblocks > 0) {
+        k_batch_collision<<<t.cblocks, kCollideThreads, 0, st>>>(t);
         nl += 1;
     }
     k_batch_flip<<<sb, 128, 0, st>>>(t);

@@ -10,12 +10,13 @@
 // interactions.  Small systems split the j range over gridDim.y blocks and
 // combine partial accelerations with float atomics before a separate
 // integrate pass.
+#include "collide_device.cuh"
 #include "tma.cuh"
 
 namespace nbgb {
 
 constexpr int kTile = 256;          // bodies per staged tile (4 KiB)
-constexpr int kDirectThreads = 256;  // collision kernel
+constexpr int kDirectThreads = 256;  // allocation-free all-pairs kernel
 constexpr int kTiledThreads = 64;    // tiled direct sum: small blocks, many per SM, even load
 
 // ---- pair interactions ----
@@ -249,74 +250,23 @@ __global__ void k_integrate_partial(DevSim s, StepParams p, const float4 *part) 
 }
 
 // ---------------------------------------------------------------------------
-// collision (update_collision_local, collision_update.cl:17-83): for every
-// body, every other body in ascending index order; if |pi - pj| <= 0.015 +
-// 0.015, reflect v_i <- v_i - 2 (n.v_i) n, n = normalize(pj - pi)
-// (calc_collision_traj, :3-15).  The running v_i carries through the j
-// order, positions are read only.  Distance and reflection use separately
-// rounded operations and a correctly rounded 1/sqrt, so every decision and
-// every result matches the oracle bit for bit.  Reads the positions written
-// by the integrator of the same step (the reference runs it after the force
-// kernel, src/MyApp.cpp:593-596).
+// collision update (update_collision_local, kernels/collision_update.cl:17-83;
+// collide_device.cuh).  It reads the positions the integrator of the same step
+// wrote, as the reference runs it after the force kernel
+// (src/MyApp.cpp:593-596).  A step that failed keeps its step-start state,
+// so the update does not run then.  Block form: one target per thread;
+// warp form (systems too small to fill the GPU with blocks): one target per
+// warp, 32 bodies tested at a time.  Both give the same bits.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kDirectThreads) k_collision(DevSim s) {
-    __shared__ __align__(128) float4 tile[2][kTile];
-    __shared__ __align__(8) uint64_t bar[2];
-    const int n = s.n;
-    const float4 *pos = s.body_next;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const float4 me = i < n ? pos[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float4 v = i < n ? s.vel[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const float rr = 0.015f + 0.015f;
-    const int ntiles = (n + kTile - 1) / kTile;
-    if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    auto issue = [&](int t, int stage) {
-        const int cnt = min(kTile, n - t * kTile);
-        const uint32_t bytes = (uint32_t)cnt * 16u;
-        mbar_expect_tx(&bar[stage], bytes);
-        bulk_g2s(&tile[stage][0], pos + (size_t)t * kTile, bytes, &bar[stage]);
-    };
-    if (threadIdx.x == 0 && ntiles > 0) issue(0, 0);
-    bool ok = true;
-    for (int t = 0; t < ntiles; ++t) {
-        const int stage = t & 1;
-        if (threadIdx.x == 0 && t + 1 < ntiles) issue(t + 1, stage ^ 1);
-        if (!mbar_wait_bounded(&bar[stage], (uint32_t)((t >> 1) & 1), s.ctrl)) ok = false;
-        const int cnt = min(kTile, n - t * kTile);
-        for (int j = 0; j < cnt; ++j) {
-            const int jj = t * kTile + j;
-            const float4 q = tile[stage][j];
-            if (jj == i) continue;
-            const float ex = __fsub_rn(me.x, q.x), ey = __fsub_rn(me.y, q.y), ez = __fsub_rn(me.z, q.z);
-            const float dist = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez)));
-            if (dist > rr) continue;
-            float nx = __fsub_rn(q.x, me.x), ny = __fsub_rn(q.y, me.y), nz = __fsub_rn(q.z, me.z);
-            const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
-            if (l2 != 0.0f) {
-                const float inv = __fdiv_rn(1.0f, __fsqrt_rn(l2));
-                nx = __fmul_rn(nx, inv);
-                ny = __fmul_rn(ny, inv);
-                nz = __fmul_rn(nz, inv);
-            }
-            const float dp = __fadd_rn(__fadd_rn(__fmul_rn(nx, v.x), __fmul_rn(ny, v.y)), __fmul_rn(nz, v.z));
-            const float k2 = __fmul_rn(2.0f, dp);
-            v.x = __fsub_rn(v.x, __fmul_rn(k2, nx));
-            v.y = __fsub_rn(v.y, __fmul_rn(k2, ny));
-            v.z = __fsub_rn(v.z, __fmul_rn(k2, nz));
-        }
-        if (!__syncthreads_and(ok)) {
-            if (threadIdx.x == 0 && t + 1 < ntiles)
-                mbar_wait_bounded(&bar[stage ^ 1], (uint32_t)(((t + 1) >> 1) & 1), s.ctrl);
-            ok = false;
-            break;
-        }
-    }
-    if (ok && i < n) s.vel[i] = v;
+__global__ void __launch_bounds__(kCollideThreads) k_collision(DevSim s, const int *order) {
+    if (read_status(s.ctrl)) return;  // block-uniform, before any barrier
+    collide_block(s.body_next, s.vel, order, s.n, blockIdx.x * kCollideThreads, s.ctrl);
+}
+
+__global__ void __launch_bounds__(kCollideWarps * 32) k_collision_warp(DevSim s) {
+    if (read_status(s.ctrl)) return;  // warp-uniform
+    const int lane = threadIdx.x & 31;
+    collide_warp(s.body_next, s.vel, s.n, blockIdx.x * kCollideWarps + (threadIdx.x >> 5), lane);
 }
 
 __global__ void k_copy_vertices(const float4 *__restrict__ b, int n, float4 *__restrict__ dst) {
@@ -494,9 +444,12 @@ cudaError_t launch_direct(const DevSim &s, const StepParams &p, int tiled, int q
     }
 }
 
-cudaError_t launch_collision(const DevSim &s, int sm_count, cudaStream_t st) {
-    (void)sm_count;
-    k_collision<<<(s.n + kDirectThreads - 1) / kDirectThreads, kDirectThreads, 0, st>>>(s);
+cudaError_t launch_collision(const DevSim &s, int tree, int sm_count, cudaStream_t st) {
+    const int blocks = (s.n + kCollideThreads - 1) / kCollideThreads;
+    if (blocks < collide_warp_form_below(sm_count))
+        k_collision_warp<<<(s.n + kCollideWarps - 1) / kCollideWarps, kCollideWarps * 32, 0, st>>>(s);
+    else
+        k_collision<<<blocks, kCollideThreads, 0, st>>>(s, tree ? s.sorted : nullptr);
     return cudaGetLastError();
 }
 

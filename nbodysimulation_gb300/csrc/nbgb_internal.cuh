@@ -20,6 +20,8 @@
 namespace nbgb {
 
 constexpr int kMaxDepth = 64;
+// targets per block of the collision update's block form (one thread each)
+constexpr int kCollideBlockBodies = 256;
 constexpr int kLocked = -2;
 constexpr int kEmpty = -1;
 
@@ -191,6 +193,8 @@ struct SysDesc {
     int cell_begin;    // prefix over BH systems' cell slots (cap + 1)
     int group_begin;   // prefix over BH systems' warp groups
     int dblock_begin;  // prefix over direct systems' target blocks
+    int cblock_begin;  // prefix over colliding systems' collision blocks
+    int collide;       // the collision update runs after the force and integrate stages
     int chunk;         // bodies per bbox / build block (batch_chunk)
     TopTables top;     // top-level tables; levels = 0: insertions from the root
 };
@@ -199,8 +203,8 @@ struct SysDesc {
 struct BatchTables {
     const SysDesc *sys;
     int nsys;
-    const int *chunk_prefix, *cell_prefix, *group_prefix, *dblock_prefix;
-    int chunks, cells, groups, dblocks;
+    const int *chunk_prefix, *cell_prefix, *group_prefix, *dblock_prefix, *cblock_prefix;
+    int chunks, cells, groups, dblocks, cblocks;
     int *work;         // batch-wide force work counter
     int *used_prefix;  // nsys + 1: prefix over the cells each tree allocated this step (device-written)
 };
@@ -246,7 +250,8 @@ cudaError_t launch_sort(const DevSim &s, int sm_count, cudaStream_t st);
 cudaError_t launch_force(const DevSim &s, const StepParams &p, int compensated, int sm_count, cudaStream_t st);
 cudaError_t launch_direct(const DevSim &s, const StepParams &p, int tiled, int quirk, int sm_count,
                           cudaStream_t st);
-cudaError_t launch_collision(const DevSim &s, int sm_count, cudaStream_t st);
+// tree != 0: s.sorted holds this step's in-order sort (targets handed out in it)
+cudaError_t launch_collision(const DevSim &s, int tree, int sm_count, cudaStream_t st);
 cudaError_t launch_copy_vertices(const float4 *body, int n, float4 *dst, cudaStream_t st);
 cudaError_t launch_pack(const float *pos3, const float *mass, const float *vel3, float4 *body, float4 *vel,
                         float4 *acc, int n, cudaStream_t st);

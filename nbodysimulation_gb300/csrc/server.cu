@@ -104,7 +104,7 @@ struct nb_server {
     int *d_pref[2] = {nullptr, nullptr}, *h_pref[2] = {nullptr, nullptr};
     int *d_work = nullptr;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
-    int exec_totals[2][5] = {};
+    int exec_totals[2][kBatchSpaces + 1] = {};
     cudaEvent_t round_ev[2] = {nullptr, nullptr};
 
     std::string err;
@@ -288,16 +288,16 @@ static cudaError_t launch_round(nb_server *s, std::vector<JobP> &run, int steps,
                                 std::deque<Delivery> &outs, std::vector<JobP> &finished) {
     const int ns = (int)run.size();
     for (int k = 0; k < ns; ++k) s->h_sys[buf][k] = run[k]->desc;
-    int totals[4];
+    int totals[kBatchSpaces];
     batch_prefixes(s->h_sys[buf], ns, batch_direct_block_bodies(s->variant), s->h_pref[buf], totals);
     cudaError_t e;
     if ((e = cudaMemcpyAsync(s->d_sys[buf], s->h_sys[buf], sizeof(SysDesc) * ns, cudaMemcpyHostToDevice,
                              s->compute)) != cudaSuccess)
         return e;
-    if ((e = cudaMemcpyAsync(s->d_pref[buf], s->h_pref[buf], sizeof(int) * 4 * (size_t)(ns + 1),
+    if ((e = cudaMemcpyAsync(s->d_pref[buf], s->h_pref[buf], sizeof(int) * batch_prefix_ints(ns),
                              cudaMemcpyHostToDevice, s->compute)) != cudaSuccess)
         return e;
-    const int key[5] = {ns, totals[0], totals[1], totals[2], totals[3]};
+    const int key[kBatchSpaces + 1] = {ns, totals[0], totals[1], totals[2], totals[3], totals[4]};
     if (!s->exec[buf] || memcmp(key, s->exec_totals[buf], sizeof(key)) != 0) {
         // the kernels read everything else from the device tables; only the
         // totals (grid sizes) and the system count live in the graph
@@ -558,9 +558,9 @@ nb_status nb_server_create(const nb_server_config *c, nb_job_fn fn, void *user, 
               cudaMalloc(&s->d_work, sizeof(int)) == cudaSuccess;
     for (int b = 0; b < 2 && ok; ++b) {
         ok = cudaMalloc(&s->d_sys[b], sizeof(SysDesc) * ns) == cudaSuccess &&
-             cudaMalloc(&s->d_pref[b], sizeof(int) * 5 * (ns + 1)) == cudaSuccess &&
+             cudaMalloc(&s->d_pref[b], sizeof(int) * batch_prefix_device_ints((int)ns)) == cudaSuccess &&
              cudaMallocHost(&s->h_sys[b], sizeof(SysDesc) * ns) == cudaSuccess &&
-             cudaMallocHost(&s->h_pref[b], sizeof(int) * 4 * (ns + 1)) == cudaSuccess &&
+             cudaMallocHost(&s->h_pref[b], sizeof(int) * batch_prefix_ints((int)ns)) == cudaSuccess &&
              cudaEventCreateWithFlags(&s->round_ev[b], cudaEventDisableTiming) == cudaSuccess;
     }
     if (!ok) return bad(NB_ERR_OUT_OF_MEMORY);
@@ -579,7 +579,7 @@ nb_status nb_server_submit(nb_server *s, const nb_config *cfg, int32_t steps, fl
         return NB_ERR_INVALID_ARGUMENT;
     if (pos3 && !mass) return NB_ERR_INVALID_ARGUMENT;
     if (c.numerical_method != s->cfg.numerical_method || c.precision != s->cfg.precision ||
-        c.multipole != s->cfg.multipole || c.collision || c.device != s->cfg.device)
+        c.multipole != s->cfg.multipole || c.device != s->cfg.device)
         return NB_ERR_UNSUPPORTED;
     if (c.algo_config != NB_BARNES_HUT && c.force_law != NB_FORCE_PLUMMER) return NB_ERR_UNSUPPORTED;
     const float eps =

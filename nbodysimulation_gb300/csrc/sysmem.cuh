@@ -130,17 +130,27 @@ inline SysDesc sysmem_desc(const SysMem &m, const nb_config &c, float dt) {
     p.quadrupole = m.quad ? 1 : 0;
     p.eps = m.tree ? c.epsilon : (c.direct_epsilon >= 0.0f ? c.direct_epsilon : c.epsilon);
     d.kind = m.tree ? kSysBH : kSysDirect;
+    d.collide = c.collision ? 1 : 0;
     d.active = 1;
     return d;
 }
 
-// Where every system's work starts in the four batch-wide index spaces
-// (bbox/build chunks, cell slots, force warp groups, direct-sum blocks of
-// `direct_block` bodies).  Fills the *_begin fields of sys, the four prefix
-// tables (nsys + 1 entries each, back to back in pref) and their totals.
-inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, int totals[4]) {
-    int *chunk = pref, *cell = pref + (nsys + 1), *group = pref + 2 * (nsys + 1), *dblock = pref + 3 * (nsys + 1);
-    chunk[0] = cell[0] = group[0] = dblock[0] = 0;
+// The batch-wide index spaces: bbox/build chunks, cell slots, force warp
+// groups, direct-sum blocks, collision blocks.
+constexpr int kBatchSpaces = 5;
+// host-written prefix tables, nsys + 1 entries each
+inline size_t batch_prefix_ints(int nsys) { return (size_t)kBatchSpaces * (size_t)(nsys + 1); }
+// on the device they are followed by the device-written table of used cells
+inline size_t batch_prefix_device_ints(int nsys) { return (size_t)(kBatchSpaces + 1) * (size_t)(nsys + 1); }
+
+// Where every system's work starts in the batch-wide index spaces (direct-sum
+// blocks of `direct_block` bodies, collision blocks of kCollideBlockBodies).
+// Fills the *_begin fields of sys, the prefix tables (nsys + 1 entries each,
+// back to back in pref) and their totals.
+inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, int totals[kBatchSpaces]) {
+    int *chunk = pref, *cell = pref + (nsys + 1), *group = pref + 2 * (nsys + 1), *dblock = pref + 3 * (nsys + 1),
+        *cblock = pref + 4 * (nsys + 1);
+    chunk[0] = cell[0] = group[0] = dblock[0] = cblock[0] = 0;
     long long tree_bodies = 0;
     for (int k = 0; k < nsys; ++k)
         if (sys[k].active && sys[k].kind == kSysBH) tree_bodies += sys[k].v.n;
@@ -153,23 +163,27 @@ inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, 
         d.cell_begin = cell[k];
         d.group_begin = group[k];
         d.dblock_begin = dblock[k];
+        d.cblock_begin = cblock[k];
         const bool bh = d.active && d.kind == kSysBH, direct = d.active && d.kind == kSysDirect;
         d.chunk = batch_chunk(n, tree_bodies);
         chunk[k + 1] = chunk[k] + (bh ? (n + d.chunk - 1) / d.chunk : 0);
         cell[k + 1] = cell[k] + (bh ? d.v.cap + 1 : 0);
         group[k + 1] = group[k] + (bh ? (n + 31) / 32 : 0);
         dblock[k + 1] = dblock[k] + (direct ? (n + direct_block - 1) / direct_block : 0);
+        cblock[k + 1] = cblock[k] + (d.active && d.collide ? (n + kCollideBlockBodies - 1) / kCollideBlockBodies : 0);
         body += n;
     }
     totals[0] = chunk[nsys];
     totals[1] = cell[nsys];
     totals[2] = group[nsys];
     totals[3] = dblock[nsys];
+    totals[4] = cblock[nsys];
 }
 
-// d_pref holds the four prefix tables of batch_prefixes followed by room for
-// the device-written table of used cells: 5 * (nsys + 1) ints.
-inline BatchTables batch_tables(const SysDesc *d_sys, int nsys, int *d_pref, const int totals[4], int *work) {
+// d_pref holds the prefix tables of batch_prefixes followed by room for the
+// device-written table of used cells: batch_prefix_device_ints(nsys) ints.
+inline BatchTables batch_tables(const SysDesc *d_sys, int nsys, int *d_pref, const int totals[kBatchSpaces],
+                                int *work) {
     BatchTables t{};
     t.sys = d_sys;
     t.nsys = nsys;
@@ -177,12 +191,14 @@ inline BatchTables batch_tables(const SysDesc *d_sys, int nsys, int *d_pref, con
     t.cell_prefix = d_pref + (nsys + 1);
     t.group_prefix = d_pref + 2 * (nsys + 1);
     t.dblock_prefix = d_pref + 3 * (nsys + 1);
+    t.cblock_prefix = d_pref + 4 * (nsys + 1);
     t.chunks = totals[0];
     t.cells = totals[1];
     t.groups = totals[2];
     t.dblocks = totals[3];
+    t.cblocks = totals[4];
     t.work = work;
-    t.used_prefix = d_pref + 4 * (nsys + 1);
+    t.used_prefix = d_pref + kBatchSpaces * (nsys + 1);
     return t;
 }
 

@@ -126,6 +126,48 @@ def test_reference_tree_semantics_match_standalone(gpu):
                 np.testing.assert_array_equal(a, r, err_msg=f"system {k} {what}")
 
 
+def test_collision_in_a_batch_matches_standalone(gpu, oracle):
+    """Systems with collision = 1 in a batch run the same collision update as
+    a standalone handle after their integration: tree systems (gravity on)
+    and direct systems (gravity off, so both paths integrate the same
+    positions) equal nb_step on standalone handles bit for bit, next to a
+    system without collisions; the direct system also equals the oracle's
+    integrate-then-collide."""
+    nb = gpu
+    specs = [(20000, True, 1.0, 0.08), (3000, False, 0.0, 0.03), (9001, True, 1.0, 0.05), (40000, False, 0.0, 0.1),
+             (5000, True, 1.0, 0.05)]
+    cfgs, states = [], []
+    for k, (n, bh, G, sigma) in enumerate(specs):
+        c = cfg(nb, n, bh)
+        c.gravitational_constant = G
+        c.collision = 0 if k == 4 else 1
+        cfgs.append(c)
+        states.append((normal(n, 900 + k, (sigma, sigma, sigma)), lognormal_mass(n, 900 + k),
+                       (10 * small_vel(n, 900 + k)).astype(np.float32)))
+    dt, steps = 1e-3, 3
+    with nb.Batch(cfgs) as b:
+        for k, (p, m, v) in enumerate(states):
+            b.set_state(k, p, m, v)
+        b.step(dt, steps)
+        got = [b.get_state(k) for k in range(len(cfgs))]
+    for k, (p, m, v) in enumerate(states):
+        ref = standalone(nb, cfgs[k], p, m, v, dt, steps)
+        for a, r, what in zip(got[k][:2], ref[:2], ("pos", "vel")):
+            np.testing.assert_array_equal(a, r, err_msg=f"system {k} {what}")
+    # the direct system without gravity against the oracle, step by step
+    p, m, v = states[1]
+    x, u, a = p.copy(), v.copy(), np.zeros_like(p)
+    moved = False
+    for _ in range(steps):
+        x, u, a = oracle.integrate(oracle.EULER, x, u, np.zeros_like(x), a, dt)
+        u2 = oracle.collision(x, u)
+        moved |= bool(np.any(u2 != u))
+        u = u2
+    assert moved  # contacts happened
+    np.testing.assert_array_equal(got[1][0], x)
+    np.testing.assert_array_equal(got[1][1], u)
+
+
 def test_direct_systems_against_oracle(gpu, oracle):
     nb = gpu
     sizes = [257, 1000, 2048, 5]

@@ -255,10 +255,13 @@ def test_integrators(gpu, oracle, method):
     assert np.max(np.abs(vg - v)) < 1e-5 * np.std(v)
 
 
-def test_collision_bit_exact(gpu, oracle):
+@pytest.mark.parametrize("n,sigma", [(3000, 0.05), (700, 0.02), (40000, 0.12), (65537, 0.15)])
+def test_collision_bit_exact(gpu, oracle, n, sigma):
+    """The collision update alone (no gravity, dt = 0) equals the oracle's
+    ordered reflections bit for bit: small systems take the warp form (one
+    target per warp), large ones the block form (one target per thread)."""
     nb = gpu
-    n = 3000
-    pos = normal(n, 77, (0.05, 0.05, 0.05))
+    pos = normal(n, 77, (sigma, sigma, sigma))
     mass = masses(n, 77)
     vel = (np.random.default_rng(2).normal(size=(n, 3)) * 0.1).astype(np.float32)
     sim = nb.Simulation(num_of_bodies=n, algo_config=nb.BRUTE_FORCE_GLOBAL, collision=1, gravitational_constant=0.0)

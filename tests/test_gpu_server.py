@@ -95,6 +95,29 @@ def test_same_alone_and_in_mix(gpu):
     np.testing.assert_allclose(mix_direct[0], ref[0], rtol=0, atol=1e-5)
 
 
+def test_collision_jobs_match_standalone(gpu):
+    """Jobs with collision = 1 are served (the collision update runs in the
+    batched step after their integration): a tree job equals a standalone
+    handle bit for bit, alone and next to a job without collisions."""
+    nb = gpu
+    dt = 1e-3
+    c = jcfg(nb, 12000, True)
+    c.collision = 1
+    pos, vel, mass = job_state(12000, 31)
+    state = (0.06 * pos, 10 * vel, mass)  # dense enough for contacts
+    other = jcfg(nb, 30000, True)
+    with nb.Server() as srv:
+        jo = srv.submit(other, 40, dt, *[job_state(30000, 32)[i] for i in (0, 2, 1)])
+        j = srv.submit(c, 25, dt, state[0], state[2], state[1])
+        assert srv.wait(-1, WAIT_S) == 0
+        got = srv.result(j, 12000)
+    ref = standalone(nb, c, 25, dt, state)
+    np.testing.assert_array_equal(got[0], ref[0])
+    np.testing.assert_array_equal(got[1], ref[1])
+    no_coll = standalone(nb, jcfg(nb, 12000, True), 25, dt, state)
+    assert np.any(no_coll[1] != ref[1])  # the collisions changed the velocities
+
+
 def test_snapshots_every_k_steps(gpu):
     nb = gpu
     dt = 1e-3
