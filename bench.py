@@ -911,7 +911,10 @@ def run_serve(args, dist: Dist):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded job stream; initial conditions generated by the server)",
-        "config": {"workload": SERVE["name"], "rate_jobs_per_s": args.serve_rate,
+        "config": {"workload": f"serve_poisson{args.serve_rate:g}_{args.serve_seconds:g}s_n1k_1m",
+                   "stream": (f"the first {args.serve_seconds:g} s of the configuration's 60 s of arrivals (60 s offer "
+                              f"about 5e11 body-updates: over 10 minutes of GPU time per arm at these rates)"),
+                   "rate_jobs_per_s": args.serve_rate,
                    "stream_seconds": args.serve_seconds, "jobs": len(jobs),
                    "n_range": [SERVE["n_min"], SERVE["n_max"]], "steps_range": [SERVE["steps_min"], SERVE["steps_max"]],
                    "thetas": list(SERVE["thetas"]), "eps": SERVE["eps"], "dt": SERVE["dt"],
