@@ -694,6 +694,7 @@ def run_batch(args, dist: Dist):
         b.set_state(k, p, m, v)
     cache = os.path.join(ROOT, "nbodysimulation_gb300", "_build", "autotune.json")
     variant = b.autotune(cache)
+    shape = b.tree_shape()
     b.step(dt, args.warmup)
     steps = args.batch_steps
     clocks = ClockSampler(dev)
@@ -758,7 +759,7 @@ def run_batch(args, dist: Dist):
         "config": {"workload": BATCH["name"], "systems": len(cfgs), "bodies": bodies, "tree_systems": n_bh,
                    "direct_systems": len(cfgs) - n_bh, "direct_below": BATCH["direct_below"],
                    "theta": BATCH["theta"], "eps": BATCH["eps"], "dt": dt, "G": BATCH["G"], "integrator": "euler",
-                   "precision": "fp32", "multipole": "monopole", "direct_variant": variant,
+                   "precision": "fp32", "multipole": "monopole", "direct_variant": variant, "tree_shape": shape,
                    "launches_per_step": info["launches_per_step"],
                    "l2": "inputs larger than L2 (all systems' bodies and trees, several GB)",
                    "parallelism": f"replicas x{dist.world}"},

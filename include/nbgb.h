@@ -343,10 +343,18 @@ nb_status nb_batch_step(nb_batch *b, float dt, int32_t nsteps);
 nb_status nb_batch_time_steps(nb_batch *b, float dt, int32_t nsteps, float *total_ms);
 /* Status of system k after the last nb_batch_step. */
 nb_status nb_batch_system_status(nb_batch *b, int32_t k);
-/* Chooses the direct-sum kernel shape by timing the candidates on this
- * batch (state unchanged); the choice is cached in the JSON file cache_path
- * (may be NULL) under a key of the SM count and the batch's size profile. */
+/* Chooses launch shapes by timing candidates on this batch with dt = 0
+ * (positions, velocities and accelerations unchanged): the direct-sum kernel
+ * shape (*chosen) and the tree stages' shape (nb_batch_tree_shape).  The
+ * choices are cached in the JSON file cache_path (may be NULL) under keys of
+ * the SM count and the batch's size profile (and, for the tree stages, its
+ * multipole and precision).  No shape changes a result: a tuned batch's
+ * systems stay bit-identical to standalone handles for the tree path. */
 nb_status nb_batch_autotune(nb_batch *b, const char *cache_path, int32_t *chosen);
+/* The tree stages' launch shape: warps per block of the force walk, percent
+ * of its resident blocks launched, bodies per bbox / build block (0: the
+ * default rule) and the cap on the top levels built before the insertions. */
+nb_status nb_batch_tree_shape(nb_batch *b, int32_t out[4]);
 /* out: systems, bodies, tree systems, direct systems, launches per step,
  * direct variant, kernels launched so far, body-node interactions of the
  * last step (tree systems). */

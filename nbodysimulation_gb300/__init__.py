@@ -121,6 +121,7 @@ SIGNATURES = {
     "nb_batch_system_status": ([_P, _I], _I),
     "nb_batch_autotune": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
     "nb_batch_info": ([_P, _P], _I),
+    "nb_batch_tree_shape": ([_P, _P], _I),
     "nb_batch_last_error_message": ([_P], ctypes.c_char_p),
     "nb_snapshot_write": ([ctypes.c_char_p, ctypes.c_int64, _D, _P, _P, _P, _I], _I),
     "nb_snapshot_read": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_D), _P, _P, _P, _I,
@@ -405,6 +406,14 @@ class Batch:
         path = None if cache_path is None else os.fsencode(cache_path)
         self._check(self.L.nb_batch_autotune(self.h, path, ctypes.byref(chosen)), "nb_batch_autotune")
         return chosen.value
+
+    def tree_shape(self):
+        """The tree stages' launch shape: force warps per block, percent of the
+        resident force blocks, build chunk (0: default rule), top-level cap."""
+        out = np.zeros(4, np.int32)
+        self._check(self.L.nb_batch_tree_shape(self.h, out.ctypes.data), "nb_batch_tree_shape")
+        keys = ("force_warps", "force_grid_pct", "build_chunk", "top_levels")
+        return dict(zip(keys, (int(x) for x in out)))
 
     def info(self):
         out = np.zeros(8, np.int64)

@@ -40,6 +40,7 @@ struct nb_batch {
     BatchTables t{};
     int method = NB_EULER, comp = 0, quad = 0;
     int variant = 5;
+    TreeShape shape{};  // launch shapes of the tree stages (autotuned)
     float dt = NAN;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -74,12 +75,18 @@ static void drop_graph(nb_batch *b) {
     b->graph = nullptr;
 }
 
-// Work offsets of every system in the batch-wide index spaces.
+// Work offsets of every system in the batch-wide index spaces, with the
+// tree shape's top-level cap and build chunk applied.
 static nb_status rebuild_tables(nb_batch *b) {
     const int ns = b->nsys;
+    for (int k = 0; k < ns; ++k)
+        if (b->h_sys[k].kind == kSysBH)
+            sysdesc_set_top(b->h_sys[k], b->mem[k], b->cfg[k].tree_semantics == NB_TREE_REFERENCE,
+                            b->shape.top_levels);
     std::vector<int> pref(batch_prefix_ints(ns), 0);
     int totals[kBatchSpaces];
-    batch_prefixes(b->h_sys.data(), ns, batch_direct_block_bodies(b->variant), pref.data(), totals);
+    batch_prefixes(b->h_sys.data(), ns, batch_direct_block_bodies(b->variant), pref.data(), totals,
+                   b->shape.build_chunk);
     B_CUDA(b, cudaMemcpyAsync(b->d_sys, b->h_sys.data(), sizeof(SysDesc) * ns, cudaMemcpyHostToDevice, b->st));
     B_CUDA(b, cudaMemcpyAsync(b->d_pref, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, b->st));
     B_CUDA(b, cudaStreamSynchronize(b->st));
@@ -333,7 +340,8 @@ static nb_status enqueue_steps(nb_batch *b, float dt, int nsteps) {
         // the device, so the same graph serves every step
         B_CUDA(b, cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
         int nl = 0;
-        cudaError_t e = launch_batch_step(b->t, b->method, b->comp, b->quad, b->variant, b->sm, b->st, &b->fork, &nl);
+        cudaError_t e = launch_batch_step(b->t, b->method, b->comp, b->quad, b->variant, b->shape, b->sm, b->st,
+                                          &b->fork, &nl);
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(b->st, &g);
         if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -398,87 +406,252 @@ nb_status nb_batch_system_status(nb_batch *b, int32_t k) {
     return (nb_status)b->h_ctrl[k].status;
 }
 
+// Velocities and accelerations of the systems of one kind, saved before
+// the autotuner's dt = 0 runs and put back after them (those runs rewrite the
+// accelerations, and v + a * 0 can turn a -0 velocity into +0).
+struct SavedState {
+    float4 *buf = nullptr;
+    size_t bodies = 0;
+};
+
+static cudaError_t move_state(nb_batch *b, int kind, SavedState &sv, bool save) {
+    size_t o = 0;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < b->nsys && e == cudaSuccess; ++k) {
+        if (b->h_sys[k].kind != kind) continue;
+        const size_t n = (size_t)b->mem[k].n, bytes = sizeof(float4) * n;
+        float4 *v = sv.buf + o, *a = sv.buf + sv.bodies + o;
+        if (save) {
+            e = cudaMemcpyAsync(v, b->mem[k].vel, bytes, cudaMemcpyDeviceToDevice, b->st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(a, b->mem[k].acc, bytes, cudaMemcpyDeviceToDevice, b->st);
+        } else {
+            e = cudaMemcpyAsync(b->mem[k].vel, v, bytes, cudaMemcpyDeviceToDevice, b->st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(b->mem[k].acc, a, bytes, cudaMemcpyDeviceToDevice, b->st);
+        }
+        o += n;
+    }
+    return e;
+}
+
+static cudaError_t save_state(nb_batch *b, int kind, SavedState &sv) {
+    sv.bodies = 0;
+    for (int k = 0; k < b->nsys; ++k)
+        if (b->h_sys[k].kind == kind) sv.bodies += (size_t)b->mem[k].n;
+    cudaError_t e = cudaMalloc(&sv.buf, sizeof(float4) * 2 * (sv.bodies > 0 ? sv.bodies : 1));
+    return e == cudaSuccess ? move_state(b, kind, sv, true) : e;
+}
+
+static cudaError_t restore_state(nb_batch *b, int kind, SavedState &sv) {
+    cudaError_t e = move_state(b, kind, sv, false);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    cudaFree(sv.buf);
+    sv.buf = nullptr;
+    return e;
+}
+
+// The candidates of the tree stages' launch shapes; the cache keeps the
+// chosen shape as one integer of their indices.
+static const int kTuneWarps[] = {2, 4, 8};
+static const int kTunePct[] = {100, 75, 50};
+static const int kTuneChunk[] = {0, 1024, 2048, 4096};  // 0: batch_chunk's rule
+static const int kTuneLevels[] = {4, 3, 2, 0};
+static_assert(kBatchTopMaxLevels == 4, "kTuneLevels starts at the largest level count");
+
+static int shape_code(const TreeShape &t) {
+    auto idx = [](const int *a, int n, int v) {
+        for (int i = 0; i < n; ++i)
+            if (a[i] == v) return i;
+        return 0;
+    };
+    return idx(kTuneWarps, 3, t.force_warps) + 3 * idx(kTunePct, 3, t.force_grid_pct) +
+           9 * idx(kTuneChunk, 4, t.build_chunk) + 36 * idx(kTuneLevels, 4, t.top_levels);
+}
+
+static bool shape_from_code(int c, TreeShape &t) {
+    if (c < 0 || c >= 3 * 3 * 4 * 4) return false;
+    t.force_warps = kTuneWarps[c % 3];
+    t.force_grid_pct = kTunePct[(c / 3) % 3];
+    t.build_chunk = kTuneChunk[(c / 9) % 4];
+    t.top_levels = kTuneLevels[c / 36];
+    return true;
+}
+
+static std::string tree_tune_key(const nb_batch *b) {
+    std::map<int, int> hist;  // log2 size bucket of the tree systems
+    for (int k = 0; k < b->nsys; ++k)
+        if (b->h_sys[k].kind == kSysBH) hist[(int)std::floor(std::log2((double)b->mem[k].n))] += 1;
+    std::ostringstream os;
+    os << "batch_tree/sm" << b->sm << "/quad" << b->quad << "/comp" << b->comp;
+    for (auto &kv : hist) os << "/" << kv.first << "x" << kv.second;
+    return os.str();
+}
+
+// Device time of 3 steps (after one warm-up) with the batch's current
+// direct variant and tree shape, without the collision update and the flip:
+// the tree stages and the direct sums beside them, captured into a CUDA graph
+// and replayed as a step is (measured: the same kernels issued one by one on
+// the streams schedule differently, and ranked the build chunks the other
+// way round).  dt is 0 in every system's parameters.
+static cudaError_t time_shapes(nb_batch *b, float *ms) {
+    cudaError_t e = launch_batch_clear(b->t, b->st);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+    int nl = 0;
+    const cudaError_t le = launch_batch_step(b->t, b->method, b->comp, b->quad, b->variant, b->shape, b->sm, b->st,
+                                             &b->fork, &nl, false);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->st, &g);
+    if (le != cudaSuccess) e = le;
+    cudaGraphExec_t x = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&x, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e == cudaSuccess) e = cudaGraphLaunch(x, b->st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->e0, b->st);
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) e = cudaGraphLaunch(x, b->st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->e1, b->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b->e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, b->e0, b->e1);
+    if (x) cudaGraphExecDestroy(x);
+    b->launches += 4 * (long long)nl;
+    // a trial in which a system failed skipped work: its time means nothing
+    if (e == cudaSuccess) e = cudaMemcpy(b->h_ctrl, b->d_ctrl, sizeof(Ctrl) * b->nsys, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        for (int k = 0; k < b->nsys; ++k)
+            if (b->h_ctrl[k].status != 0) *ms = INFINITY;
+    return e;
+}
+
+// One pass of coordinate descent over the four shape parameters (top-level
+// cap, build chunk, warps per block, grid fraction), each timed in whole
+// steps of this batch; every shape gives the same results, only the time
+// differs.
+static nb_status tune_tree_shape(nb_batch *b, TreeShape &best) {
+    SavedState sv, sv_d;
+    cudaError_t e = save_state(b, kSysBH, sv);
+    if (e == cudaSuccess) e = save_state(b, kSysDirect, sv_d);
+    if (e != cudaSuccess) {
+        cudaFree(sv.buf);
+        cudaFree(sv_d.buf);
+        return bfail(b, NB_ERR_CUDA, std::string("autotune save: ") + cudaGetErrorString(e));
+    }
+    const float keep_dt = b->dt;
+    for (auto &d : b->h_sys) d.p.dt = 0.0f;
+    best = b->shape;
+    float best_ms = INFINITY;
+    nb_status r = NB_OK;
+    auto trial = [&](const TreeShape &t) {
+        if (r != NB_OK || e != cudaSuccess) return;
+        b->shape = t;
+        if ((r = rebuild_tables(b)) != NB_OK) return;
+        float ms = 0.0f;
+        e = time_shapes(b, &ms);
+        if (e == cudaSuccess && ms < best_ms) {
+            best_ms = ms;
+            best = t;
+        }
+    };
+    trial(best);
+    for (int v : kTuneLevels) { TreeShape t = best; t.top_levels = v; if (v != best.top_levels) trial(t); }
+    for (int v : kTuneChunk) { TreeShape t = best; t.build_chunk = v; if (v != best.build_chunk) trial(t); }
+    for (int v : kTuneWarps) { TreeShape t = best; t.force_warps = v; if (v != best.force_warps) trial(t); }
+    for (int v : kTunePct) { TreeShape t = best; t.force_grid_pct = v; if (v != best.force_grid_pct) trial(t); }
+    for (auto &d : b->h_sys) d.p.dt = keep_dt;
+    b->dt = keep_dt;
+    b->shape = best;
+    cudaError_t er = restore_state(b, kSysBH, sv);
+    const cudaError_t er2 = restore_state(b, kSysDirect, sv_d);
+    if (er == cudaSuccess) er = er2;
+    if (r != NB_OK) return r;
+    if (e != cudaSuccess || er != cudaSuccess)
+        return bfail(b, NB_ERR_CUDA,
+                     std::string("autotune (tree shapes): ") + cudaGetErrorString(e != cudaSuccess ? e : er));
+    return rebuild_tables(b);
+}
+
 nb_status nb_batch_autotune(nb_batch *b, const char *cache_path, int32_t *chosen) {
     if (!b) return NB_ERR_INVALID_ARGUMENT;
     cudaSetDevice(b->dev);
-    const std::string key = tune_key(b);
     std::map<std::string, int> cache = read_cache(cache_path);
+    bool dirty = false;
+    // --- the direct-sum kernel shape ---
+    const std::string key = tune_key(b);
     int best = b->variant;
-    bool have_direct = false;
-    for (auto &d : b->h_sys) have_direct |= d.kind == kSysDirect && d.active;
+    bool have_direct = false, have_tree = false;
+    for (auto &d : b->h_sys) {
+        have_direct |= d.kind == kSysDirect && d.active;
+        have_tree |= d.kind == kSysBH && d.active;
+    }
     auto it = cache.find(key);
     if (!have_direct) {
         best = b->variant;
     } else if (it != cache.end() && it->second >= 0 && it->second < batch_direct_variants()) {
         best = it->second;
     } else {
-        // time every variant on this batch with dt = 0: positions and
-        // velocities stay as they are, and the accelerations the runs
-        // overwrite (the first half-kick of the next leapfrog step reads
-        // them) are saved before and put back after
-        size_t acc_n = 0;
-        for (int k = 0; k < b->nsys; ++k)
-            if (b->h_sys[k].kind == kSysDirect) acc_n += (size_t)b->mem[k].n;
-        float4 *saved = nullptr;
-        B_CUDA(b, cudaMalloc(&saved, sizeof(float4) * acc_n));
-        auto move_acc = [&](bool save) {
-            size_t o = 0;
-            cudaError_t e = cudaSuccess;
-            for (int k = 0; k < b->nsys && e == cudaSuccess; ++k) {
-                if (b->h_sys[k].kind != kSysDirect) continue;
-                const size_t bytes = sizeof(float4) * (size_t)b->mem[k].n;
-                e = save ? cudaMemcpyAsync(saved + o, b->mem[k].acc, bytes, cudaMemcpyDeviceToDevice, b->st)
-                         : cudaMemcpyAsync(b->mem[k].acc, saved + o, bytes, cudaMemcpyDeviceToDevice, b->st);
-                o += (size_t)b->mem[k].n;
-            }
-            return e;
-        };
-        cudaError_t e = move_acc(true);
+        // time every variant on this batch with dt = 0 in whole steps (the
+        // direct sums run beside the tree stages): positions stay as they
+        // are, and the velocities and accelerations the runs rewrite are
+        // saved before and put back after
+        SavedState sv_d, sv_t;
+        cudaError_t e = save_state(b, kSysDirect, sv_d);
+        if (e == cudaSuccess) e = save_state(b, kSysBH, sv_t);
         if (e != cudaSuccess) {
-            cudaFree(saved);
+            cudaFree(sv_d.buf);
+            cudaFree(sv_t.buf);
             return bfail(b, NB_ERR_CUDA, std::string("autotune save: ") + cudaGetErrorString(e));
         }
         const float keep = b->dt;
-        for (auto &d : b->h_sys) d.p.dt = 0.0f;
         float best_ms = INFINITY;
         nb_status r = NB_OK;
         for (int v = 0; v < batch_direct_variants() && r == NB_OK && e == cudaSuccess; ++v) {
             b->variant = v;
             for (auto &d : b->h_sys) d.p.dt = 0.0f;
             if ((r = rebuild_tables(b)) != NB_OK) break;
-            e = launch_batch_direct_only(b->t, v, b->st);  // warm-up
-            if (e == cudaSuccess) e = cudaEventRecord(b->e0, b->st);
-            for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) e = launch_batch_direct_only(b->t, v, b->st);
-            if (e == cudaSuccess) e = cudaEventRecord(b->e1, b->st);
-            if (e == cudaSuccess) e = cudaEventSynchronize(b->e1);
             float ms = 0.0f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->e0, b->e1);
-            b->launches += 4;
+            e = time_shapes(b, &ms);
             if (e == cudaSuccess && ms < best_ms) {
                 best_ms = ms;
                 best = v;
             }
         }
-        if (r != NB_OK || e != cudaSuccess) {
-            for (auto &d : b->h_sys) d.p.dt = keep;
-            move_acc(false);
-            cudaStreamSynchronize(b->st);
-            cudaFree(saved);
-            if (r != NB_OK) return r;
-            return bfail(b, NB_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
-        }
         for (auto &d : b->h_sys) d.p.dt = keep;
-        e = move_acc(false);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
-        cudaFree(saved);
-        if (e != cudaSuccess) return bfail(b, NB_ERR_CUDA, std::string("autotune restore: ") + cudaGetErrorString(e));
+        const cudaError_t er = restore_state(b, kSysDirect, sv_d);
+        const cudaError_t er2 = restore_state(b, kSysBH, sv_t);
+        if (r != NB_OK) return r;
+        if (e != cudaSuccess || er != cudaSuccess || er2 != cudaSuccess)
+            return bfail(b, NB_ERR_CUDA,
+                         std::string("autotune: ") +
+                             cudaGetErrorString(e != cudaSuccess ? e : (er != cudaSuccess ? er : er2)));
         cache[key] = best;
-        write_cache(cache_path, cache);
+        dirty = true;
     }
     b->variant = best;
     nb_status r = rebuild_tables(b);
     if (r != NB_OK) return r;
+    // --- the tree stages' launch shapes ---
+    if (have_tree) {
+        const std::string tkey = tree_tune_key(b);
+        auto ti = cache.find(tkey);
+        TreeShape shape;
+        if (ti != cache.end() && shape_from_code(ti->second, shape)) {
+            b->shape = shape;
+            if ((r = rebuild_tables(b)) != NB_OK) return r;
+        } else {
+            if ((r = tune_tree_shape(b, shape)) != NB_OK) return r;
+            cache[tkey] = shape_code(shape);
+            dirty = true;
+        }
+    }
+    if (dirty) write_cache(cache_path, cache);
     if (chosen) *chosen = best;
+    return NB_OK;
+}
+
+nb_status nb_batch_tree_shape(nb_batch *b, int32_t out[4]) {
+    if (!b || !out) return NB_ERR_INVALID_ARGUMENT;
+    out[0] = b->shape.force_warps;
+    out[1] = b->shape.force_grid_pct;
+    out[2] = b->shape.build_chunk;
+    out[3] = b->shape.top_levels;
     return NB_OK;
 }
 

@@ -262,25 +262,36 @@ __global__ void __launch_bounds__(256) k_batch_sort(BatchTables t) {
 // thresholds whenever its next group belongs to another system.  A system
 // whose step failed keeps its step-start state.
 // ---------------------------------------------------------------------------
+// Shared memory of one warp of the batched force kernel.  The block has a
+// runtime number of warps (TreeShape::force_warps), so the warps' records are
+// laid out one after another in dynamic shared memory.
+template <bool kQuad>
+struct BatchForceWarp {
+    float dq[kMaxDepth];
+    int stack[kStack];
+    float4 bpm[32], cpm[32], cmeta[32], cqa[kQuad ? 32 : 1];
+    // the current system's buffers and parameters: the walk reads them from
+    // shared memory where the single-system kernel reads its kernel
+    // parameters, instead of holding them in registers
+    DevSim view;
+    StepParams par;
+    // the current system, its first group and its mode (0 walk, 1 keep the
+    // step-start state of a failed step, 2 inert): in shared memory, so
+    // nothing of the outer loop stays live in registers during a walk
+    int cur, begin, mode;
+};
+constexpr int kBatchForceMaxWarps = 8;
+
 template <int kMethod, bool kComp, bool kQuad>
-__global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
-    __shared__ float s_dq[kForceWarps][kMaxDepth];
-    __shared__ int s_stack[kForceWarps][kStack];
-    __shared__ float4 s_bpm[kForceWarps][32];
-    __shared__ float4 s_cpm[kForceWarps][32];
-    __shared__ float4 s_cmeta[kForceWarps][32];
-    __shared__ float4 s_cqa[kForceWarps][kQuad ? 32 : 1];
-    // the current system's buffers and parameters, one copy per warp: the
-    // walk reads them from shared memory where the single-system kernel reads
-    // its kernel parameters, instead of holding them in registers
-    __shared__ DevSim s_view[kForceWarps];
-    __shared__ StepParams s_par[kForceWarps];
-    // the current system of each warp, its first group and its mode (0 walk,
-    // 1 keep the step-start state of a failed step, 2 inert): in shared
-    // memory, so nothing of the outer loop stays live in registers during a walk
-    __shared__ int s_cur[kForceWarps], s_begin[kForceWarps], s_mode[kForceWarps];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) s_cur[w] = -1;
+__global__ void __launch_bounds__(kBatchForceMaxWarps * 32) k_batch_force(BatchTables t) {
+    extern __shared__ __align__(16) unsigned char force_smem[];
+    BatchForceWarp<kQuad> &me = reinterpret_cast<BatchForceWarp<kQuad> *>(force_smem)[threadIdx.x >> 5];
+    float *const s_dq_w = me.dq;
+    DevSim &s_view_w = me.view;
+    StepParams &s_par_w = me.par;
+    int &s_cur_w = me.cur, &s_begin_w = me.begin, &s_mode_w = me.mode;
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) s_cur_w = -1;
     __syncwarp();
     while (true) {
         int gg = 0;
@@ -288,15 +299,15 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
         gg = __shfl_sync(0xffffffffu, gg, 0);
         if (gg >= t.groups) break;
         const int k = find_system(t.group_prefix, t.nsys, gg);
-        if (k != s_cur[w]) {
+        if (k != s_cur_w) {
             __syncwarp();  // the previous system's view and thresholds are no longer read
             if (lane == 0) {
                 const SysDesc &d = t.sys[k];
                 const DevSim v = system_view(d);
                 StepParams p = d.p;
                 p.kdk_primed = v.ctrl->kdk_primed;
-                s_view[w] = v;
-                s_par[w] = p;
+                s_view_w = v;
+                s_par_w = p;
                 int sk = 0;
                 if (!system_live(v.ctrl)) {
                     sk = 2;
@@ -308,24 +319,24 @@ __global__ void __launch_bounds__(kForceThreads) k_batch_force(BatchTables t) {
                 }
                 float box[6];
                 load_box(v.ctrl, box);
-                make_thresholds(box, p.theta, p.eps, p.crit_ref, s_dq[w]);
-                s_cur[w] = k;
-                s_begin[w] = d.group_begin;
-                s_mode[w] = sk;
+                make_thresholds(box, p.theta, p.eps, p.crit_ref, s_dq_w);
+                s_cur_w = k;
+                s_begin_w = d.group_begin;
+                s_mode_w = sk;
             }
             __syncwarp();
         }
-        const int g = gg - s_begin[w];
-        const int mode = s_mode[w];
-        const DevSim &s = s_view[w];
+        const int g = gg - s_begin_w;
+        const int mode = s_mode_w;
+        const DevSim &s = s_view_w;
         if (mode == 2) continue;
         if (mode == 1) {  // keep the step-start state
             const int i = g * 32 + lane;
             if (i < s.n) s.body_next[i] = s.body_cur[i];
             continue;
         }
-        const WarpStage ws{s_stack[w], s_bpm[w], s_cpm[w], s_cmeta[w], s_cqa[w]};
-        force_group<kMethod, kComp, false, kQuad>(s, s_par[w], s_dq[w], g, lane, ws);
+        const WarpStage ws{me.stack, me.bpm, me.cpm, me.cmeta, me.cqa};
+        force_group<kMethod, kComp, false, kQuad>(s, s_par_w, s_dq_w, g, lane, ws);
     }
 }
 
@@ -495,28 +506,75 @@ static cudaError_t launch_direct_variant(const BatchTables &t, int variant, cuda
     return cudaGetLastError();
 }
 
-template <int kMethod>
-static cudaError_t launch_batch_force_m(const BatchTables &t, int comp, int quad, int sm_count, cudaStream_t st) {
-    const void *fn;
-    if (quad) fn = comp ? (const void *)k_batch_force<kMethod, true, true> : (const void *)k_batch_force<kMethod, false, true>;
-    else fn = comp ? (const void *)k_batch_force<kMethod, true, false> : (const void *)k_batch_force<kMethod, false, false>;
-    int blocks = resident(fn, kForceThreads, sm_count);
-    const int need = (t.groups + kForceWarps - 1) / kForceWarps;
-    if (blocks > need) blocks = need > 0 ? need : 1;
-    if (quad) {
-        if (comp) k_batch_force<kMethod, true, true><<<blocks, kForceThreads, 0, st>>>(t);
-        else k_batch_force<kMethod, false, true><<<blocks, kForceThreads, 0, st>>>(t);
-    } else {
-        if (comp) k_batch_force<kMethod, true, false><<<blocks, kForceThreads, 0, st>>>(t);
-        else k_batch_force<kMethod, false, false><<<blocks, kForceThreads, 0, st>>>(t);
-    }
+template <int kMethod, bool kComp, bool kQuad>
+static cudaError_t launch_batch_force_t(const BatchTables &t, const TreeShape &shape, int sm_count,
+                                        cudaStream_t st) {
+    int warps = shape.force_warps;
+    if (warps < 1 || warps > kBatchForceMaxWarps) warps = kForceWarps;
+    const int threads = warps * 32;
+    const size_t smem = sizeof(BatchForceWarp<kQuad>) * (size_t)warps;
+    const void *fn = (const void *)k_batch_force<kMethod, kComp, kQuad>;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    long long blocks = (long long)per_sm * sm_count * (shape.force_grid_pct > 0 ? shape.force_grid_pct : 100) / 100;
+    const int need = (t.groups + warps - 1) / warps;
+    if (blocks > need) blocks = need;
+    if (blocks < 1) blocks = 1;
+    k_batch_force<kMethod, kComp, kQuad><<<(int)blocks, threads, smem, st>>>(t);
     return cudaGetLastError();
 }
+
+template <int kMethod>
+static cudaError_t launch_batch_force_m(const BatchTables &t, int comp, int quad, const TreeShape &shape,
+                                        int sm_count, cudaStream_t st) {
+    if (quad) return comp ? launch_batch_force_t<kMethod, true, true>(t, shape, sm_count, st)
+                          : launch_batch_force_t<kMethod, false, true>(t, shape, sm_count, st);
+    return comp ? launch_batch_force_t<kMethod, true, false>(t, shape, sm_count, st)
+                : launch_batch_force_t<kMethod, false, false>(t, shape, sm_count, st);
+}
+
+// bbox .. force of every tree system; *launches gets the kernel count
+static cudaError_t launch_batch_tree_stages(const BatchTables &t, int method, int comp, int quad,
+                                            const TreeShape &shape, int sm_count, cudaStream_t st,
+                                            const StepFork *fork, bool branch, int *launches) {
+    cudaError_t e = cudaSuccess;
+    const int sb = (t.nsys + 127) / 128;
+    k_batch_reset<<<sb, 128, 0, st>>>(t);
+    k_batch_bbox<<<t.chunks, 256, 0, st>>>(t);
+    k_batch_top_count<<<t.chunks, 256, 0, st>>>(t);
+    k_batch_top_cells<<<t.nsys, 256, 0, st>>>(t);
+    k_batch_build<<<t.chunks, 256, 0, st>>>(t);
+    k_batch_used<<<1, kScanThreads, 0, st>>>(t);
+    // many blocks, so the grid-stride tail is short (512 systems: 8 per SM
+    // 4.79 ms, 32 per SM 2.90 ms)
+    int sblocks = sm_count * 32;
+    const int need = (t.cells + 255) / 256;
+    if (sblocks > need) sblocks = need;
+    if (quad) k_batch_summarize<true><<<sblocks, 256, 0, st>>>(t);
+    else k_batch_summarize<false><<<sblocks, 256, 0, st>>>(t);
+    if (branch && (e = cudaStreamWaitEvent(st, fork->join, 0)) != cudaSuccess) return e;
+    int rblocks = resident((const void *)k_batch_sort, 256, sm_count);
+    if (rblocks > need) rblocks = need;
+    k_batch_sort<<<rblocks, 256, 0, st>>>(t);
+    if ((e = cudaMemsetAsync(t.work, 0, sizeof(int), st)) != cudaSuccess) return e;
+    switch (method) {
+    case 1: e = launch_batch_force_m<1>(t, comp, quad, shape, sm_count, st); break;
+    case 2: e = launch_batch_force_m<2>(t, comp, quad, shape, sm_count, st); break;
+    case 3: e = launch_batch_force_m<3>(t, comp, quad, shape, sm_count, st); break;
+    default: e = launch_batch_force_m<0>(t, comp, quad, shape, sm_count, st); break;
+    }
+    if (launches) *launches = 9;
+    return e;
+}
+
+
 
 // One batched step.  Kernels with no work in this batch are not launched.
 // Returns the number of kernels launched through *launches.
 cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int quad, int direct_variant,
-                              int sm_count, cudaStream_t st, const StepFork *fork, int *launches) {
+                              const TreeShape &shape, int sm_count, cudaStream_t st, const StepFork *fork,
+                              int *launches, bool advance) {
     int nl = 0;
     cudaError_t e = cudaSuccess;
     const int sb = (t.nsys + 127) / 128;
@@ -530,36 +588,19 @@ cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int qu
         nl += 1;
     }
     if (t.chunks > 0) {
-        k_batch_reset<<<sb, 128, 0, st>>>(t);
-        k_batch_bbox<<<t.chunks, 256, 0, st>>>(t);
-        k_batch_top_count<<<t.chunks, 256, 0, st>>>(t);
-        k_batch_top_cells<<<t.nsys, 256, 0, st>>>(t);
-        k_batch_build<<<t.chunks, 256, 0, st>>>(t);
-        k_batch_used<<<1, kScanThreads, 0, st>>>(t);
-        // many blocks, so the grid-stride tail is short (512 systems: 8 per SM
-        // 4.79 ms, 32 per SM 2.90 ms)
-        int sblocks = sm_count * 32;
-        const int need = (t.cells + 255) / 256;
-        if (sblocks > need) sblocks = need;
-        if (quad) k_batch_summarize<true><<<sblocks, 256, 0, st>>>(t);
-        else k_batch_summarize<false><<<sblocks, 256, 0, st>>>(t);
-        if (branch && (e = cudaStreamWaitEvent(st, fork->join, 0)) != cudaSuccess) return e;
-        int rblocks = resident((const void *)k_batch_sort, 256, sm_count);
-        if (rblocks > need) rblocks = need;
-        k_batch_sort<<<rblocks, 256, 0, st>>>(t);
-        if ((e = cudaMemsetAsync(t.work, 0, sizeof(int), st)) != cudaSuccess) return e;
-        switch (method) {
-        case 1: e = launch_batch_force_m<1>(t, comp, quad, sm_count, st); break;
-        case 2: e = launch_batch_force_m<2>(t, comp, quad, sm_count, st); break;
-        case 3: e = launch_batch_force_m<3>(t, comp, quad, sm_count, st); break;
-        default: e = launch_batch_force_m<0>(t, comp, quad, sm_count, st); break;
-        }
-        if (e != cudaSuccess) return e;
-        nl += 9;
+        int tl = 0;
+        if ((e = launch_batch_tree_stages(t, method, comp, quad, shape, sm_count, st, fork, branch, &tl)) !=
+            cudaSuccess)
+            return e;
+        nl += tl;
     }
     if (t.dblocks > 0 && !branch) {
         if ((e = launch_direct_variant(t, direct_variant, st)) != cudaSuccess) return e;
         nl += 1;
+    }
+    if (!advance) {
+        if (launches) *launches = nl;
+        return cudaGetLastError();
     }
     if (t.cblocks > 0) {
         k_batch_collision<<<t.cblocks, kCollideThreads, 0, st>>>(t);
@@ -585,12 +626,6 @@ __global__ void k_batch_clear(BatchTables t) {
 cudaError_t launch_batch_clear(const BatchTables &t, cudaStream_t st) {
     k_batch_clear<<<(t.nsys + 127) / 128, 128, 0, st>>>(t);
     return cudaGetLastError();
-}
-
-// The direct-sum kernel alone, for the autotuner.
-cudaError_t launch_batch_direct_only(const BatchTables &t, int variant, cudaStream_t st) {
-    if (t.dblocks <= 0) return cudaSuccess;
-    return launch_direct_variant(t, variant, st);
 }
 
 }  // namespace nbgb

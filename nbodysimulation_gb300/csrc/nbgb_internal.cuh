@@ -285,9 +285,21 @@ struct StepFork {
     cudaStream_t aux;
     cudaEvent_t fork, join;
 };
+// Launch shapes of a batched step that do not change any result (the tree
+// and every sum are the same for all of them), so the autotuner may choose
+// them and a batched system stays bit-identical to a standalone handle.
+struct TreeShape {
+    int force_warps = 4;       // warps per block of the batched force kernel: 2, 4 or 8
+    int force_grid_pct = 100;  // percent of the resident force blocks launched
+    int build_chunk = 0;       // bodies per bbox / build block of every tree; 0: batch_chunk's rule
+    int top_levels = kBatchTopMaxLevels;  // at most this many top levels built first
+};
+// advance = false leaves out the collision update and the flip: the tree
+// stages and the direct sums as a step runs them (the direct sums beside the
+// tree stages on fork->aux), which is what the autotuner times with dt = 0.
 cudaError_t launch_batch_step(const BatchTables &t, int method, int comp, int quad, int direct_variant,
-                              int sm_count, cudaStream_t st, const StepFork *fork, int *launches);
-cudaError_t launch_batch_direct_only(const BatchTables &t, int variant, cudaStream_t st);
+                              const TreeShape &shape, int sm_count, cudaStream_t st, const StepFork *fork,
+                              int *launches, bool advance = true);
 // clears the status word and work counters of every system (once per call)
 cudaError_t launch_batch_clear(const BatchTables &t, cudaStream_t st);
 

@@ -307,7 +307,8 @@ static cudaError_t launch_round(nb_server *s, std::vector<JobP> &run, int steps,
         const int quad = s->cfg.multipole == NB_MULTIPOLE_QUADRUPOLE;
         if ((e = cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
         int nl = 0;
-        cudaError_t le = launch_batch_step(t, method, comp, quad, s->variant, s->sm, s->cap, &s->fork, &nl);
+        cudaError_t le = launch_batch_step(t, method, comp, quad, s->variant, TreeShape{}, s->sm, s->cap, &s->fork,
+                                           &nl);
         cudaGraph_t g = nullptr;
         e = cudaStreamEndCapture(s->cap, &g);
         if (le != cudaSuccess) e = le;

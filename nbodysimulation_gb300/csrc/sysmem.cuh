@@ -91,6 +91,17 @@ inline size_t sysmem_bytes(int n, bool tree, bool quad, int cap) {
 
 // Descriptor of a system: its buffers and the step parameters of its config
 // (the same choices as the standalone step).
+// The top-level tables of a system building min(m.top_levels, cap) top
+// levels (none for the reference tree semantics, which always insert from
+// the root).  The count table (8^levels entries, zero between steps) and the
+// start table lie at fixed places for any level count -- the start table
+// after room for the counts of m.top_levels -- so a step with fewer levels
+// never leaves start entries where a later step with more levels counts.
+inline void sysdesc_set_top(SysDesc &d, const SysMem &m, bool tree_ref, int cap) {
+    const int top = tree_ref ? 0 : (m.top_levels < cap ? m.top_levels : cap);
+    d.top = TopTables{top ? m.top : nullptr, top ? m.top + (1 << (3 * m.top_levels)) : nullptr, top};
+}
+
 inline SysDesc sysmem_desc(const SysMem &m, const nb_config &c, float dt) {
     SysDesc d{};
     DevSim &v = d.v;
@@ -114,9 +125,7 @@ inline SysDesc sysmem_desc(const SysMem &m, const nb_config &c, float dt) {
     v.wqa = m.wqa;
     v.wqb = m.wqb;
     v.ctrl = m.ctrl;
-    // the reference tree semantics always insert from the root
-    const int top = c.tree_semantics == NB_TREE_REFERENCE ? 0 : m.top_levels;
-    d.top = TopTables{top ? m.top : nullptr, top ? m.top + (1 << (3 * top)) : nullptr, top};
+    sysdesc_set_top(d, m, c.tree_semantics == NB_TREE_REFERENCE, kBatchTopMaxLevels);
     d.body[0] = m.body[0];
     d.body[1] = m.body[1];
     StepParams &p = d.p;
@@ -144,10 +153,12 @@ inline size_t batch_prefix_ints(int nsys) { return (size_t)kBatchSpaces * (size_
 inline size_t batch_prefix_device_ints(int nsys) { return (size_t)(kBatchSpaces + 1) * (size_t)(nsys + 1); }
 
 // Where every system's work starts in the batch-wide index spaces (direct-sum
-// blocks of `direct_block` bodies, collision blocks of kCollideBlockBodies).
+// blocks of `direct_block` bodies, collision blocks of kCollideBlockBodies,
+// bbox / build chunks of chunk_override bodies when > 0, else batch_chunk's).
 // Fills the *_begin fields of sys, the prefix tables (nsys + 1 entries each,
 // back to back in pref) and their totals.
-inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, int totals[kBatchSpaces]) {
+inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, int totals[kBatchSpaces],
+                           int chunk_override = 0) {
     int *chunk = pref, *cell = pref + (nsys + 1), *group = pref + 2 * (nsys + 1), *dblock = pref + 3 * (nsys + 1),
         *cblock = pref + 4 * (nsys + 1);
     chunk[0] = cell[0] = group[0] = dblock[0] = cblock[0] = 0;
@@ -165,7 +176,7 @@ inline void batch_prefixes(SysDesc *sys, int nsys, int direct_block, int *pref, 
         d.dblock_begin = dblock[k];
         d.cblock_begin = cblock[k];
         const bool bh = d.active && d.kind == kSysBH, direct = d.active && d.kind == kSysDirect;
-        d.chunk = batch_chunk(n, tree_bodies);
+        d.chunk = chunk_override > 0 ? chunk_override : batch_chunk(n, tree_bodies);
         chunk[k + 1] = chunk[k] + (bh ? (n + d.chunk - 1) / d.chunk : 0);
         cell[k + 1] = cell[k] + (bh ? d.v.cap + 1 : 0);
         group[k + 1] = group[k] + (bh ? (n + 31) / 32 : 0);

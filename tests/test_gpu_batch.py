@@ -235,6 +235,58 @@ def test_autotune_cache_and_unchanged_state(gpu, tmp_path):
             np.testing.assert_array_equal(x, y)
 
 
+@pytest.mark.parametrize("method,precision,quad", [(3, 0, 0), (2, 1, 1)])
+def test_autotune_tree_shapes(gpu, tmp_path, method, precision, quad):
+    """The tree stages' launch shapes (force warps per block, force grid,
+    build chunk, top-level cap) are timed on the batch with dt = 0: the
+    state is bit for bit the same after tuning, the choice is one of the
+    candidates and is read back from the cache, and a tuned batch steps its
+    tree systems exactly as an untuned batch and as standalone handles (no
+    shape changes a result)."""
+    nb = gpu
+    specs = [(20000, True), (3000, False), (70000, True), (9001, True), (140000, True)]
+    cfgs = [cfg(nb, n, bh, method, precision, quad) for n, bh in specs]
+    states = [(normal(n, 300 + k), lognormal_mass(n, 300 + k), small_vel(n, 300 + k))
+              for k, (n, _) in enumerate(specs)]
+    cache = tmp_path / "tune.json"
+    dt = 1e-3
+
+    def run(tune):
+        with nb.Batch(cfgs) as b:
+            for k, (p, m, v) in enumerate(states):
+                b.set_state(k, p, m, v)
+            b.step(dt, 1)
+            before = [b.get_state(k) for k in range(len(specs))]
+            shape = None
+            if tune:
+                b.autotune(str(cache))
+                shape = b.tree_shape()
+                after = [b.get_state(k) for k in range(len(specs))]
+                for k, (x, y) in enumerate(zip(before, after)):
+                    for u, w, what in zip(x, y, ("pos", "vel", "acc", "mass")):
+                        np.testing.assert_array_equal(u, w, err_msg=f"tuning changed system {k} {what}")
+            b.step(dt, 2)
+            return shape, [b.get_state(k) for k in range(len(specs))]
+
+    shape, tuned = run(True)
+    assert shape["force_warps"] in (2, 4, 8) and shape["force_grid_pct"] in (100, 75, 50)
+    assert shape["build_chunk"] in (0, 1024, 2048, 4096) and shape["top_levels"] in (0, 2, 3, 4)
+    table = json.loads(cache.read_text())
+    assert any(k.startswith("batch_tree/") for k in table) and any(k.startswith("batch_direct/") for k in table)
+    shape2, again = run(True)  # read back from the cache
+    assert shape2 == shape
+    _, plain = run(False)
+    for k, (n, bh) in enumerate(specs):
+        if not bh:
+            continue
+        ref = standalone(nb, cfgs[k], *states[k], dt, 3)
+        for a, b_, r, what in zip(tuned[k][:3], plain[k][:3], ref[:3], ("pos", "vel", "acc")):
+            np.testing.assert_array_equal(a, b_, err_msg=f"system {k} {what}: tuned vs untuned batch")
+            np.testing.assert_array_equal(a, r, err_msg=f"system {k} {what}: tuned batch vs standalone")
+        for x, y in zip(tuned[k], again[k]):
+            np.testing.assert_array_equal(x, y)
+
+
 def test_batch_rejects_mixed_settings(gpu):
     nb = gpu
     with pytest.raises(nb.NbError) as e:
