@@ -269,7 +269,7 @@ template <bool kQuad>
 struct BatchForceWarp {
     float dq[kMaxDepth];
     int stack[kStack];
-    float4 bpm[32], cpm[32], cmeta[32], cqa[kQuad ? 32 : 1];
+    float4 bpm[8 * kBatch], cpm[8 * kBatch], cmeta[8 * kBatch], cqa[kQuad ? 8 * kBatch : 1];
     // the current system's buffers and parameters: the walk reads them from
     // shared memory where the single-system kernel reads its kernel
     // parameters, instead of holding them in registers
@@ -514,6 +514,10 @@ static cudaError_t launch_batch_force_t(const BatchTables &t, const TreeShape &s
     const int threads = warps * 32;
     const size_t smem = sizeof(BatchForceWarp<kQuad>) * (size_t)warps;
     const void *fn = (const void *)k_batch_force<kMethod, kComp, kQuad>;
+    if (smem > 48 * 1024) {  // beyond the default dynamic shared memory of a block: opt in
+        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;

@@ -9,10 +9,10 @@ template <int kMethod, bool kComp, bool kEpsZero, bool kQuad>
 __global__ void __launch_bounds__(kForceThreads) k_force(DevSim s, StepParams p) {
     __shared__ float s_dq[kMaxDepth];
     __shared__ int s_stack[kForceWarps][kStack];
-    __shared__ float4 s_bpm[kForceWarps][32];
-    __shared__ float4 s_cpm[kForceWarps][32];
-    __shared__ float4 s_cmeta[kForceWarps][32];
-    __shared__ float4 s_cqa[kForceWarps][kQuad ? 32 : 1];
+    __shared__ float4 s_bpm[kForceWarps][8 * kBatch];
+    __shared__ float4 s_cpm[kForceWarps][8 * kBatch];
+    __shared__ float4 s_cmeta[kForceWarps][8 * kBatch];
+    __shared__ float4 s_cqa[kForceWarps][kQuad ? 8 * kBatch : 1];
     __shared__ int s_skip;
     Ctrl *ctrl = s.ctrl;
     const int n = s.n;
