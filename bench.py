@@ -13,7 +13,8 @@ accumulation, seeded synthetic data.  Metric: body-updates/s.
 resident in HBM; `e2e` goes through the public C ABI every step:
 nb_set_state from pinned host arrays, nb_step, nb_get_state into pinned host
 arrays (page-locked: the library's kernels read and write them across the host
-link in place, with no staging copy).  The accuracy gate (RMS relative force error vs an FP64 direct sum
+link in place, with no staging copy); `e2e.host_link` measures the link's
+width for the same bytes and the transfer floor it sets.  The accuracy gate (RMS relative force error vs an FP64 direct sum
 on 8192 sample bodies <= 1e-3) is evaluated after the timed region.
 
 The same line carries more measurements, each with its own timed region
@@ -297,6 +298,35 @@ def stage_roofline(stage_ms, n, cells, hbm_gbs, quad=True):
     return out
 
 
+def host_link(dev, h2d_bytes, d2h_bytes, reps=5):
+    """Width of the host link for one step's transfers: copy-engine copies
+    between page-locked host buffers and device buffers of the e2e step's
+    sizes, timed with CUDA events on the copying stream after 3 warm-up
+    copies.  Kernels that read or write page-locked host arrays in place
+    (nb_set_state / nb_get_state) run at the same width on this link, so
+    bytes / width is the floor of the transfer part of an e2e step."""
+    import torch
+    out = {}
+    with torch.cuda.device(dev):
+        for name, nbytes, to_dev in (("h2d", h2d_bytes, True), ("d2h", d2h_bytes, False)):
+            h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+            d = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{dev}")
+            src, dst = (h, d) if to_dev else (d, h)
+            for _ in range(3):
+                dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                dst.copy_(src, non_blocking=True)
+            b.record()
+            b.synchronize()
+            out[f"{name}_gbs"] = nbytes * reps / (a.elapsed_time(b) * 1e6)
+            del h, d
+    out["transfer_floor_ms_per_step"] = (h2d_bytes / out["h2d_gbs"] + d2h_bytes / out["d2h_gbs"]) / 1e6
+    return out
+
+
 def run_ours(args, dist: Dist):
     from nbodysimulation_gb300 import build as nbbuild
     if dist.local_rank == 0:
@@ -353,6 +383,9 @@ def run_ours(args, dist: Dist):
     for p in hp:
         L.nb_host_free(p)
     e2e_value = total_bodies * args.steps / e2e_s
+    link = host_link(dev, 28 * n, 24 * n + 64)
+    link["e2e_ms_per_step"] = e2e_s * 1e3 / args.steps
+    link["device_ms_per_step"] = ms_max / args.steps
 
     # --- accuracy gate (after the timed regions) ---
     rng = np.random.default_rng(1234)
@@ -405,7 +438,7 @@ def run_ours(args, dist: Dist):
         "data": "synthetic (seeded normal sigma=(1,1,0.2) positions, lognormal masses)",
         "config": step_config(n, dist.world),
         "e2e": {"value": e2e_value, "unit": "body-updates/s", "h2d_bytes_per_step": 28 * n,
-                "d2h_bytes_per_step": 24 * n + 64},
+                "d2h_bytes_per_step": 24 * n + 64, "host_link": link},
         "gpu_launches": int(launches),
         "stages_ms": {k: round(v, 4) for k, v in stage.items() if v > 0},
         "accuracy": {"rms_rel_err": err_rms, "max_rel_err": err_max, "samples": PROBE_SAMPLES,
