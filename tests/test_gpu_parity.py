@@ -562,6 +562,50 @@ def test_largest_tree_and_the_size_limit(gpu):
     assert e.value.status == nb.ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("n", [1, 3, 31, 32, 33, 65])
+def test_ragged_small_systems(gpu, oracle, n):
+    """Sizes around one warp group of 32 bodies, and a single body, through
+    every algorithm with and without softening: a lone body feels no force
+    and drifts with its velocity; the direct sums equal the FP64 sum within
+    1e-5 of the typical acceleration (MUFU rsqrt, FP32 sums); the tree walk
+    (monopole and quadrupole, plain and compensated) equals the oracle's
+    walk with the same votes within 2e-5 of the typical acceleration."""
+    nb = gpu
+    pos = normal(n, 500 + n)
+    mass = masses(n, 500 + n, "lognormal")
+    for eps in (0.01, 0.0):
+        ref = oracle.direct_fp64(pos, mass, eps, 1.0)
+        for algo in (nb.BRUTE_FORCE_GLOBAL, nb.BRUTE_FORCE_LOCAL):
+            with nb.Simulation(num_of_bodies=n, algo_config=algo, epsilon=eps, gravitational_constant=1.0) as sim:
+                sim.set_state(pos, mass)
+                sim.step(0.0, 1)
+                acc = sim.get_state()[2]
+            if n == 1:
+                assert np.array_equal(acc, np.zeros((1, 3), np.float32)), (algo, eps, acc)
+            else:
+                assert rel_to_typical(acc, ref) < 1e-5, (algo, eps)
+        for quad in (0, 1):
+            for comp in (0, 1):
+                want, _, _ = oracle.bh_step_forces(pos, mass, 0.5, eps, 1.0, quadrupole=bool(quad),
+                                                   compensated=bool(comp))
+                with bh_sim(nb, pos, mass, 0.5, eps, quad=quad, precision=comp) as sim:
+                    sim.step(0.0, 1)
+                    acc = sim.get_state()[2]
+                if n == 1:
+                    assert np.array_equal(acc, np.zeros((1, 3), np.float32)), (quad, comp, eps, acc)
+                else:
+                    assert rel_to_typical(acc, want) < 2e-5, (quad, comp, eps)
+    if n == 1:
+        vel = np.array([[0.5, -0.25, 2.0]], np.float32)
+        with bh_sim(nb, pos, mass, 0.5, 0.01, vel=vel) as sim:
+            sim.step(np.float32(0.125), 4)
+            p = sim.get_state()[0]
+        want = pos.copy()
+        for _ in range(4):
+            want = (want + vel * np.float32(0.125)).astype(np.float32)
+        assert np.array_equal(p, want)
+
+
 @pytest.mark.parametrize("eps", [0.01, 0.0])
 def test_theta_zero_opens_every_cell(gpu, oracle, eps):
     """theta = 0 accepts no cell, so the walk reaches every body: the
