@@ -190,6 +190,16 @@ def _f32(a, shape=None):
     return a if shape is None else a.reshape(shape)
 
 
+def _out(a, shape):
+    """A float32 C-contiguous array of `shape` to write into: the caller's
+    array `a` (reused, so its pages are already populated), or a new one."""
+    if a is None:
+        return np.zeros(shape, np.float32)
+    if a.dtype != np.float32 or a.shape != shape or not a.flags.c_contiguous or not a.flags.writeable:
+        raise ValueError(f"output array must be writeable C-contiguous float32 of shape {shape}")
+    return a
+
+
 class Simulation:
     """One system on the GPU: the handle of nb_create (CMyApp's buffers)."""
 
@@ -235,20 +245,23 @@ class Simulation:
     def init_bodies(self):
         self._check(self.L.nb_init_bodies(self.h), "nb_init_bodies")
 
-    def get_state(self):
-        pos = np.zeros((self.n, 3), np.float32)
-        vel = np.zeros((self.n, 3), np.float32)
-        acc = np.zeros((self.n, 3), np.float32)
-        mass = np.zeros(self.n, np.float32)
+    def get_state(self, out=None):
+        """(pos, vel, acc, mass); `out` = four arrays of those shapes to reuse."""
+        o = out if out is not None else (None,) * 4
+        pos, vel, acc = (_out(a, (self.n, 3)) for a in o[:3])
+        mass = _out(o[3], (self.n,))
         self._check(self.L.nb_get_state(self.h, pos.ctypes.data, vel.ctypes.data, acc.ctypes.data,
                                         mass.ctypes.data), "nb_get_state")
         return pos, vel, acc, mass
 
-    def positions(self, with_velocities=False):
+    def positions(self, with_velocities=False, out=None):
         """Positions (N,3) -- what a snapshot or a renderer reads -- and, when
-        asked, velocities."""
-        pos = np.zeros((self.n, 3), np.float32)
-        vel = np.zeros((self.n, 3), np.float32) if with_velocities else None
+        asked, velocities.  `out` = the array (or the pair) to reuse: pages
+        that the host has never touched cost several times the copy itself on
+        their first use."""
+        o = out if isinstance(out, (tuple, list)) else (out, None)
+        pos = _out(o[0], (self.n, 3))
+        vel = _out(o[1], (self.n, 3)) if with_velocities else None
         self._check(self.L.nb_get_state(self.h, pos.ctypes.data, None if vel is None else vel.ctypes.data, None,
                                         None), "nb_get_state")
         return (pos, vel) if with_velocities else pos
@@ -377,12 +390,12 @@ class Batch:
         self._check(self.L.nb_batch_set_state(self.h, k, pos.ctypes.data, None if v is None else v.ctypes.data,
                                               mass.ctypes.data), "nb_batch_set_state")
 
-    def get_state(self, k):
+    def get_state(self, k, out=None):
+        """System k's (pos, vel, acc, mass); `out` = four arrays to reuse."""
         n = self.ns[k]
-        pos = np.zeros((n, 3), np.float32)
-        vel = np.zeros((n, 3), np.float32)
-        acc = np.zeros((n, 3), np.float32)
-        mass = np.zeros(n, np.float32)
+        o = out if out is not None else (None,) * 4
+        pos, vel, acc = (_out(a, (n, 3)) for a in o[:3])
+        mass = _out(o[3], (n,))
         self._check(self.L.nb_batch_get_state(self.h, k, pos.ctypes.data, vel.ctypes.data, acc.ctypes.data,
                                               mass.ctypes.data), "nb_batch_get_state")
         return pos, vel, acc, mass

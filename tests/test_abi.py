@@ -157,6 +157,20 @@ def test_invalid_arguments_without_device(nbgb_lib):
     assert L.nb_destroy(None) == nbgb_lib.ERR_INVALID_ARGUMENT
 
 
+def test_output_arrays_are_checked(nbgb_lib):
+    """The host mirror writes state into the caller's arrays only when they
+    are writeable C-contiguous float32 of the right shape."""
+    nb = nbgb_lib
+    a = np.zeros((4, 3), np.float32)
+    assert nb._out(a, (4, 3)) is a
+    assert nb._out(None, (4,)).shape == (4,)
+    ro = np.zeros((4, 3), np.float32)
+    ro.flags.writeable = False
+    for bad in (np.zeros((4, 3), np.float64), np.zeros((3, 4), np.float32).T, np.zeros((5, 3), np.float32), ro):
+        with pytest.raises(ValueError):
+            nb._out(bad, (4, 3))
+
+
 CPP_PROGRAM = r'''
 #include <cstdio>
 #include "nbgb.hpp"

@@ -323,6 +323,42 @@ def test_page_locked_host_arrays(gpu, oracle, n, offset):
             L.nb_host_free(p)
 
 
+def test_reused_output_arrays(gpu):
+    """get_state / positions / a batch's get_state write into the caller's
+    arrays when given them, with the same values as fresh arrays."""
+    nb = gpu
+    n = 5000
+    pos, mass = normal(n, 31), masses(n, 31, "lognormal")
+    vel = (0.1 * normal(n, 32)).astype(np.float32)
+    with bh_sim(nb, pos, mass, 0.5, 0.01, vel=vel) as sim:
+        sim.step(1e-3, 2)
+        want = sim.get_state()
+        out = tuple(np.full_like(a, np.nan) for a in want)
+        got = sim.get_state(out=out)
+        assert all(g is o for g, o in zip(got, out))
+        for g, w in zip(got, want):
+            np.testing.assert_array_equal(g, w)
+        p = np.empty((n, 3), np.float32)
+        assert sim.positions(out=p) is p
+        np.testing.assert_array_equal(p, want[0])
+        v = np.empty((n, 3), np.float32)
+        pp, vv = sim.positions(with_velocities=True, out=(p, v))
+        assert pp is p and vv is v
+        np.testing.assert_array_equal(v, want[1])
+        with pytest.raises(ValueError):
+            sim.positions(out=np.empty((n, 4), np.float32))
+    cfg = nb.default_config(num_of_bodies=n, algo_config=nb.BARNES_HUT, theta=0.5, epsilon=0.01,
+                            gravitational_constant=1.0)
+    with nb.Batch([cfg]) as b:
+        b.set_state(0, pos, mass, vel)
+        b.step(1e-3, 2)
+        out = tuple(np.full_like(a, np.nan) for a in want)
+        got = b.get_state(0, out=out)
+        assert all(g is o for g, o in zip(got, out))
+        np.testing.assert_array_equal(got[0], want[0])
+        np.testing.assert_array_equal(got[1], want[1])
+
+
 def test_known_answer_sets(gpu, oracle):
     """The hand-built sets of the oracle's known-answer tests
     (test_oracle_analytic.py) through the C ABI: two-body forces against the
