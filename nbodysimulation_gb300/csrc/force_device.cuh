@@ -98,6 +98,53 @@ struct WarpStage {
     float4 *cqa;    // {q_xx, q_yy, q_zz, q_xy}
 };
 
+// The nc cells staged this round, in order: accumulated into (sx, sy, sz)
+// when every lane accepts, else pushed.  kChecked: the round's pushes may
+// fill the stack, so each push tests for room and a cell beyond the bound
+// is dropped with the depth status (the walk's result is then discarded);
+// otherwise every push fits and the test is left out of the loop.
+template <bool kQuad, bool kChecked>
+__device__ __forceinline__ void cell_list(const float4 *cpm, const float4 *cmeta, const float4 *cqa, int nc,
+                                          const float4 P, float eps2, float &sx, float &sy, float &sz, int *stack,
+                                          int &sp, unsigned &n_drop, int lane, Ctrl *ctrl) {
+    for (int k = 0; k < nc; ++k) {
+        const float4 q = cpm[k];
+        const float4 mt = cmeta[k];
+        const float dx = q.x - P.x, dy = q.y - P.y, dz = q.z - P.z;
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+        if (__all_sync(0xffffffffu, d2 >= mt.z)) {
+            const float r = rsqrt_fast(d2);
+            const float r2 = r * r;
+            if constexpr (kQuad) {
+                // m d / r^3 + 2.5 (d.Q.d) d / r^7 - Q d / r^5
+                //   = (d (m d^2 + 2.5 (d.Q.d) / r^2) - Q d) / r^5, with r^-2 = d^2:
+                // 24 FP32 operations instead of 26
+                const float4 Q = cqa[k];  // xx yy zz xy; mt.x = xz, mt.y = yz
+                const float qx = fmaf(mt.x, dz, fmaf(Q.w, dy, Q.x * dx));
+                const float qy = fmaf(mt.y, dz, fmaf(Q.y, dy, Q.w * dx));
+                const float qz = fmaf(Q.z, dz, fmaf(mt.y, dy, mt.x * dx));
+                const float sq = fmaf(dz, qz, fmaf(dy, qy, dx * qx));
+                const float r5 = r * (r2 * r2);
+                const float t = fmaf(2.5f * sq, r2, q.w * d2);
+                sx = fmaf(fmaf(dx, t, -qx), r5, sx);
+                sy = fmaf(fmaf(dy, t, -qy), r5, sy);
+                sz = fmaf(fmaf(dz, t, -qz), r5, sz);
+            } else {
+                const float F = q.w * (r * r2);
+                sx = fmaf(dx, F, sx);
+                sy = fmaf(dy, F, sy);
+                sz = fmaf(dz, F, sz);
+            }
+        } else if (!kChecked || sp < kStack) {
+            if (lane == 0) stack[sp] = __float_as_int(mt.w);
+            ++sp;
+        } else {  // outside the stack bound: never overrun shared memory
+            ++n_drop;
+            if (lane == 0) set_status(ctrl, kStDepth, kStack);
+        }
+    }
+}
+
 // Walk of warp group g of system s (dq: its 64 thresholds), with the fused
 // integrator.  All 32 lanes call it together.
 template <int kMethod, bool kComp, bool kEpsZero, bool kQuad>
@@ -117,7 +164,7 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
     const int b = s.sorted[valid ? sidx : g * 32];
     const float4 P = s.body_cur[b];
     float ax = 0.0f, ay = 0.0f, az = 0.0f, lx = 0.0f, ly = 0.0f, lz = 0.0f;
-    unsigned n_body = 0, n_cell = 0, n_open = 0;
+    unsigned n_body = 0, n_cell = 0, n_open = 0, n_drop = 0;  // n_cell: staged cells
     int sp = 1;
     if (lane == 0) stack[0] = root;  // level 0
     __syncwarp();
@@ -178,7 +225,7 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
         float &sx = kComp ? bx : ax, &sy = kComp ? by : ay, &sz = kComp ? bz : az;
         // child bodies: always accumulated
         n_body += nb;
-#pragma unroll 2
+#pragma unroll 4
         for (int k = 0; k < nb; ++k) {
             const float4 q = bpm[k];
             const float dx = q.x - P.x, dy = q.y - P.y, dz = q.z - P.z;
@@ -190,46 +237,13 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
             sy = fmaf(dy, F, sy);
             sz = fmaf(dz, F, sz);
         }
-        // child cells: accumulated when every lane accepts, else pushed (and
-        // taken off the count of cell interactions, which is rarer than adding)
+        // child cells: accumulated when every lane accepts, else pushed; the
+        // pushes of a round that cannot fill the stack skip the room test
         n_cell += nc;
-        for (int k = 0; k < nc; ++k) {
-            const float4 q = cpm[k];
-            const float4 mt = cmeta[k];
-            const float dx = q.x - P.x, dy = q.y - P.y, dz = q.z - P.z;
-            const float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-            if (__all_sync(0xffffffffu, d2 >= mt.z)) {
-                const float r = rsqrt_fast(d2);
-                const float r2 = r * r;
-                if constexpr (kQuad) {
-                    // m d / r^3 + 2.5 (d.Q.d) d / r^7 - Q d / r^5
-                    //   = (d (m d^2 + 2.5 (d.Q.d) / r^2) - Q d) / r^5, with r^-2 = d^2:
-                    // 24 FP32 operations instead of 26
-                    const float4 Q = cqa[k];  // xx yy zz xy; mt.x = xz, mt.y = yz
-                    const float qx = fmaf(mt.x, dz, fmaf(Q.w, dy, Q.x * dx));
-                    const float qy = fmaf(mt.y, dz, fmaf(Q.y, dy, Q.w * dx));
-                    const float qz = fmaf(Q.z, dz, fmaf(mt.y, dy, mt.x * dx));
-                    const float sq = fmaf(dz, qz, fmaf(dy, qy, dx * qx));
-                    const float r5 = r * (r2 * r2);
-                    const float t = fmaf(2.5f * sq, r2, q.w * d2);
-                    sx = fmaf(fmaf(dx, t, -qx), r5, sx);
-                    sy = fmaf(fmaf(dy, t, -qy), r5, sy);
-                    sz = fmaf(fmaf(dz, t, -qz), r5, sz);
-                } else {
-                    const float F = q.w * (r * r2);
-                    sx = fmaf(dx, F, sx);
-                    sy = fmaf(dy, F, sy);
-                    sz = fmaf(dz, F, sz);
-                }
-            } else if (sp < kStack) {
-                if (lane == 0) stack[sp] = __float_as_int(mt.w);
-                ++sp;
-                --n_cell;
-            } else {  // outside the stack bound: never overrun shared memory
-                --n_cell;
-                if (lane == 0) set_status(ctrl, kStDepth, kStack);
-            }
-        }
+        if (sp + nc <= kStack)
+            cell_list<kQuad, false>(cpm, cmeta, cqa, nc, P, eps2, sx, sy, sz, stack, sp, n_drop, lane, ctrl);
+        else
+            cell_list<kQuad, true>(cpm, cmeta, cqa, nc, P, eps2, sx, sy, sz, stack, sp, n_drop, lane, ctrl);
         if constexpr (kComp) {  // one TwoSum per batch into the running sum
             two_sum_add(ax, lx, bx);
             two_sum_add(ay, ly, by);
@@ -237,6 +251,9 @@ __device__ __forceinline__ void force_group(const DevSim &s, const StepParams &p
         }
         __syncwarp();
     }
+    // every pushed cell is popped once, the root is popped without a push:
+    // rejected cells = n_open - 1 + n_drop, accepted = staged - rejected
+    n_cell -= n_open - 1u + n_drop;
     if (lane == 0) {
         const unsigned lanes = (unsigned)min(32, n - g * 32);
         atomicAdd(&ctrl->interactions, (unsigned long long)(n_body + n_cell) * lanes);
