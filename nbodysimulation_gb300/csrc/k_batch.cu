@@ -282,8 +282,10 @@ struct BatchForceWarp {
 };
 constexpr int kBatchForceMaxWarps = 8;
 
+// Register budget: at most 48 a thread for the monopole walks (ten resident
+// blocks of four warps) and 64 with quadrupoles; neither spills.
 template <int kMethod, bool kComp, bool kQuad>
-__global__ void __launch_bounds__(kBatchForceMaxWarps * 32) k_batch_force(BatchTables t) {
+__global__ void __launch_bounds__(kBatchForceMaxWarps * 32, kQuad ? 4 : 5) k_batch_force(BatchTables t) {
     extern __shared__ __align__(16) unsigned char force_smem[];
     BatchForceWarp<kQuad> &me = reinterpret_cast<BatchForceWarp<kQuad> *>(force_smem)[threadIdx.x >> 5];
     float *const s_dq_w = me.dq;
