@@ -99,7 +99,7 @@ inline size_t sysmem_bytes(int n, bool tree, bool quad, int cap) {
 // never leaves start entries where a later step with more levels counts.
 inline void sysdesc_set_top(SysDesc &d, const SysMem &m, bool tree_ref, int cap) {
     const int top = tree_ref ? 0 : (m.top_levels < cap ? m.top_levels : cap);
-    d.top = TopTables{top ? m.top : nullptr, top ? m.top + (1 << (3 * m.top_levels)) : nullptr, top};
+    d.top = TopTables{top ? m.top : nullptr, top ? m.top + (1 << (3 * m.top_levels)) : nullptr, top, nullptr};
 }
 
 inline SysDesc sysmem_desc(const SysMem &m, const nb_config &c, float dt) {
