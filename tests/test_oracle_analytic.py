@@ -105,3 +105,52 @@ def test_chain_separates_at_depth_10(oracle):
     a, b = chain_expected()
     assert list(paths[2, :depth[2]]) == a and list(paths[3, :depth[3]]) == b
     assert list(paths[0, :depth[0]]) == [7] and list(paths[1, :depth[1]]) == [0, 0]
+
+
+def _cell_table(children, mass, pos, count, n, root):
+    """(mass, centre, body count) of every cell, keyed by its octant path."""
+    ch = children.reshape(-1, 8)
+    pos = pos.reshape(-1, 3)
+    out, stack = {}, [(root, ())]
+    while stack:
+        node, path = stack.pop()
+        out[path] = (float(mass[node]), tuple(float(v) for v in pos[node]), int(count[node]))
+        for s in range(8):
+            c = ch[node][s]
+            if c >= n:
+                stack.append((c, path + (s,)))
+    return out
+
+
+@pytest.mark.parametrize("semantics", ["geometric", "reference"])
+def test_tree_does_not_depend_on_insertion_order(oracle, semantics):
+    """For distinct points the octree is a function of the point set: built
+    from the bodies in a shuffled order it has the same octant path for every
+    body, the same cells with the same summaries (children are summed in slot
+    order) and the same in-order listing of the bodies.  This is what lets a
+    sequential CPU build check the concurrent GPU build."""
+    O = oracle
+    sem = O.SEM_GEOMETRIC if semantics == "geometric" else O.SEM_REFERENCE
+    n = 3000
+    rng = np.random.default_rng(17)
+    pos = (rng.normal(size=(n, 3)) * np.array([1.0, 1.0, 0.3])).astype(np.float32)
+    mass = (0.5 + rng.random(n)).astype(np.float32)
+    perm = rng.permutation(n)
+    box = O.bbox_exact(pos)
+    built = []
+    for p, m in ((pos, mass), (pos[perm], mass[perm])):
+        t = O.tree_build(sem, p, m, box)
+        assert t.status == 0
+        octant = t.children.copy()
+        assert O.saturate(t) == 0
+        paths, depth, found = O.tree_paths(octant, n, t.root)
+        assert found == n
+        srt, k = O.sort_bodies(t.children, n, t.root)
+        assert k == n
+        table = _cell_table(octant, t.mass, t.pos, t.body_count, n, t.root)
+        built.append((paths, depth, srt, table, t.root - t.bottom, t.max_depth))
+    (pa, da, sa, ta, ca, ma), (pb, db, sb, tb, cb, mb) = built
+    assert ca == cb and ma == mb
+    assert np.array_equal(pb, pa[perm]) and np.array_equal(db, da[perm])
+    assert np.array_equal(perm[sb], sa)
+    assert ta == tb
