@@ -154,3 +154,34 @@ def test_tree_does_not_depend_on_insertion_order(oracle, semantics):
     assert np.array_equal(pb, pa[perm]) and np.array_equal(db, da[perm])
     assert np.array_equal(perm[sb], sa)
     assert ta == tb
+
+
+def test_sort_lists_every_cell_contiguously(oracle):
+    """The in-order sort puts the bodies of every cell in one contiguous run
+    of the sorted order, as long as the cell's body count (so a warp group of
+    32 consecutive sorted bodies spans few cells: the walk's vote groups)."""
+    O = oracle
+    n = 4000
+    rng = np.random.default_rng(23)
+    pos = rng.normal(size=(n, 3)).astype(np.float32)
+    mass = np.full(n, 1.0 / n, np.float32)
+    t = O.tree_build(O.SEM_GEOMETRIC, pos, mass, O.bbox_exact(pos))
+    assert t.status == 0 and O.saturate(t) == 0
+    srt, k = O.sort_bodies(t.children, n, t.root)
+    assert k == n and np.array_equal(np.sort(srt), np.arange(n))
+    where = np.empty(n, np.int64)
+    where[srt] = np.arange(n)
+    ch = t.children.reshape(-1, 8)
+
+    def span(node):  # (first, last, bodies) of the node's subtree in the sorted order
+        if node < n:
+            return where[node], where[node], 1
+        lo, hi, cnt = n, -1, 0
+        for c in ch[node]:
+            if c >= 0:
+                a, b, m = span(c)
+                lo, hi, cnt = min(lo, a), max(hi, b), cnt + m
+        assert hi - lo + 1 == cnt == t.body_count[node]
+        return lo, hi, cnt
+
+    assert span(t.root) == (0, n - 1, n)
